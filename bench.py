@@ -1,0 +1,326 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 Goldilocks NTT on the large-transform workload.
+
+Workload ("large single transforms, plain per-call"): one step is a forward
+and an inverse NTT at each of n = 2^20, 2^22, 2^24 and 16,711,680
+(= 2^16*3*5*17), on seeded synthetic field elements uniform in [0, p).
+Metric: elements transformed per second (each transform counts n).
+
+  value      device-resident inputs, CUDA events on the launching stream around
+             each step, L2 flushed (256 MiB write) between steps outside the
+             timed events.
+  e2e        the same step through the public API with pinned HOST buffers
+             (gl_ntt/gl_intt with GL_MEM_HOST: H2D copy, kernels, D2H copy and
+             synchronisation inside the timed region).
+  roofline   the kernel with the largest share of device time, its algorithmic
+             bytes per launch (16 B per element per pass: one read + one write)
+             over its mean CUDA-event launch time, against the measured HBM
+             copy bandwidth.
+  cpu_baseline  the CPU oracle (a C restatement of the reference's CPU path,
+             kind "port") on the same step, transforms spread over host threads.
+
+--impl reference times the reference's CPU algorithm (the C restatement; the
+reference is Rust and no Rust toolchain exists here) on all usable host
+threads, for the same metric and workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SIZES = [1 << 20, 1 << 22, 1 << 24, 16711680]
+METRIC = "bit-exact NTT elem/s (fwd+inv at 2^20, 2^22, 2^24, 16711680)"
+UNIT = "elem/s"
+WORKLOAD = {"workload": "large single transforms, plain per-call: forward+inverse NTT at "
+                        "n=2^20, 2^22, 2^24, 16711680 (2^16*3*5*17)",
+            "sizes": SIZES, "transforms_per_step": 2 * len(SIZES),
+            "elements_per_step": 2 * sum(SIZES), "field": "Goldilocks p=2^64-2^32+1",
+            "inputs": "uniform in [0,p), seeded (gl_fill_uniform)",
+            "l2": "flushed between steps (256 MiB write, outside timed events)"}
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], None, set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names[1:], parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def ncu_traffic():
+    """Per-element DRAM traffic of each kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def cpu_oracle_step(threads):
+    """One step of the workload on the CPU oracle; returns (elements, seconds)."""
+    import numpy as np
+
+    import oracle
+    oracle.build()
+    from goldilocks_gb300 import fill_uniform
+    inputs = [fill_uniform(n, seed=0xC0 + i) for i, n in enumerate(SIZES)]
+
+    def job(args):
+        i, inv = args
+        x = inputs[i]
+        return (oracle.intt(x) if inv else oracle.ntt(x)).size
+
+    jobs = [(i, inv) for i in range(len(SIZES)) for inv in (0, 1)]
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        total = sum(ex.map(job, jobs))
+    return total, time.perf_counter() - t0
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    threads = min(len(SIZES) * 2, os.cpu_count() or 1)
+    for _ in range(args.warmup):
+        cpu_oracle_step(threads)
+    tot_el, tot_s = 0, 0.0
+    for _ in range(args.steps):
+        el, s = cpu_oracle_step(threads)
+        tot_el += el
+        tot_s += s
+    v = tot_el / tot_s
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (mod p)",
+            "data": "synthetic", "config": WORKLOAD,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "the full step: 8 transforms, one per host thread; C restatement "
+                                       "of the reference CPU algorithm (no Rust toolchain to build the "
+                                       "reference itself)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from goldilocks_gb300 import build as gbuild
+    gbuild.build()
+    import goldilocks_gb300 as gl
+    from goldilocks_gb300 import _lib as L
+
+    lib = L.load()
+    stream = torch.cuda.current_stream()
+    plans = [gl.strategy(n) for n in SIZES]
+    bufs = []
+    for i, n in enumerate(SIZES):
+        x = gl.fill_uniform(n, seed=0xBE00 + i + 16 * rank)
+        bufs.append(torch.from_numpy(x.view(np.int64)).cuda())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    elements_per_step = 2 * sum(SIZES)
+
+    def step():
+        for pl, b in zip(plans, bufs):
+            pl.ntt(b)
+            pl.intt(b)
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    lib.gl_profile_enable(1)
+    evs = []
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    for _ in range(args.steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step()
+        b.record(stream)
+        evs.append((a, b))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    total_ms = sum(a.elapsed_time(b) for a, b in evs)
+    n_ent = lib.gl_profile_read(None, 0)
+    ents = (L.ProfileEntry * max(n_ent, 1))()
+    lib.gl_profile_read(ents, n_ent)
+    lib.gl_profile_enable(0)
+    prof = [{"name": e.name.decode(), "launches": int(e.launches), "elements": int(e.elements),
+             "total_ms": float(e.total_ms)} for e in ents[:n_ent]]
+    launches = sum(p["launches"] for p in prof)
+
+    if dist:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * elements_per_step * args.steps / (total_ms * 1e-3)
+
+    # ---- end to end through the public API with pinned host buffers ----
+    hosts = []
+    for i, n in enumerate(SIZES):
+        h = torch.empty(n, dtype=torch.int64, pin_memory=True)
+        h.numpy().view(np.uint64)[:] = gl.fill_uniform(n, seed=0xE2E0 + i)
+        hosts.append(h.numpy().view(np.uint64))
+    e2e_steps = max(1, min(args.steps, 5))
+
+    def host_step():
+        for pl, h in zip(plans, hosts):
+            pl.ntt(h)
+            pl.intt(h)
+    host_step()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        host_step()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * elements_per_step * e2e_steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": 8 * elements_per_step, "d2h_bytes_per_step": 8 * elements_per_step,
+           "steps": e2e_steps, "memory": "pinned host"}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    peak, peak_kind = peaks()
+    dom = max(prof, key=lambda p: p["total_ms"]) if prof else None
+    roofline = None
+    if dom:
+        per_launch_el = dom["elements"] / dom["launches"]
+        mean_ms = dom["total_ms"] / dom["launches"]
+        achieved = 16.0 * per_launch_el / (mean_ms * 1e-3) / 1e9
+        tr = ncu_traffic().get(dom["name"])
+        roofline = {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": peak,
+                    "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                    "traffic": (tr * per_launch_el) if tr else None,
+                    "algorithmic_bytes_per_launch": 16.0 * per_launch_el,
+                    "mean_launch_ms": mean_ms,
+                    "share": dom["total_ms"] / max(sum(p["total_ms"] for p in prof), 1e-12)}
+    # whole-transform roofline: 16 B * n * passes(n) per transform, passes = ceil(log2 n / 14)
+    import math
+    alg_bytes = sum(2 * 16 * n * math.ceil(math.log2(n) / 14) for n in SIZES)
+    step_ms = total_ms / args.steps
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64 (mod p)", "data": "synthetic",
+            "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single GPU"),
+            "roofline": roofline,
+            "step_roofline": {"algorithmic_bytes_per_step": alg_bytes,
+                              "achieved_gbs": alg_bytes / (step_ms * 1e-3) / 1e9,
+                              "frac": alg_bytes / (step_ms * 1e-3) / 1e9 / peak},
+            "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+            "kernels": prof}
+    if world == 1 and not args.no_cpu_baseline:
+        threads = min(2 * len(SIZES), os.cpu_count() or 1)
+        el, s = cpu_oracle_step(threads)
+        line["cpu_baseline"] = {"value": el / s, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "one full step (8 transforms, one per thread) of the C "
+                                          "restatement of the reference CPU algorithm"}
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,80 @@
+"""ctypes binding of libgoldilocks_gpu.so (declared in include/goldilocks_gpu.h).
+
+The library is built in-tree by goldilocks_gb300.build.  There is no fallback:
+importing the package without the built library raises.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+_u64 = ctypes.c_uint64
+_u32 = ctypes.c_uint32
+_int = ctypes.c_int
+_vp = ctypes.c_void_p
+_sz = ctypes.c_size_t
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+
+# (name, restype, argtypes) for every symbol the header declares.
+SIGNATURES = [
+    ("gl_status_string", ctypes.c_char_p, [_int]),
+    ("gl_is_divisor", _int, [_u64]),
+    ("gl_split", _u64, [_u64]),
+    ("gl_next", _u64, [_u64]),
+    ("gl_divisors", _sz, [_u64p, _sz]),
+    ("gl_plan_create", _int, [_u64, ctypes.POINTER(_vp)]),
+    ("gl_plan_release", None, [_vp]),
+    ("gl_plan_len", _u64, [_vp]),
+    ("gl_plan_describe", _int, [_vp, ctypes.c_char_p, _sz]),
+    ("gl_plan_workspace_bytes", _u64, [_vp, _u64]),
+    ("gl_plan_execute", _int, [_vp, _vp, _u64, _int, _int, _vp]),
+    ("gl_plan_execute_ws", _int, [_vp, _vp, _u64, _int, _vp, _u64, _vp]),
+    ("gl_ntt", _int, [_vp, _u64, _int, _vp]),
+    ("gl_intt", _int, [_vp, _u64, _int, _vp]),
+    ("gl_clear_cache", None, []),
+    ("gl_fill_uniform", None, [_vp, _u64, _u64, _u64]),
+    ("gl_profile_enable", _int, [_int]),
+    ("gl_profile_read", _int, [_vp, _int]),
+]
+
+
+class ProfileEntry(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 48), ("launches", ctypes.c_uint64),
+                ("elements", ctypes.c_uint64), ("total_ms", ctypes.c_double)]
+
+GL_OK = 0
+GL_ERR_UNSUPPORTED_SIZE = 1
+GL_ERR_INVALID = 2
+GL_ERR_OOM = 3
+GL_ERR_BUDGET = 4
+GL_ERR_TIMEOUT = 5
+GL_ERR_CUDA = 6
+GL_ERR_BUSY = 7
+GL_ERR_CANCELLED = 8
+GL_ERR_NOT_FOUND = 9
+GL_FORWARD, GL_INVERSE = 0, 1
+GL_MEM_HOST, GL_MEM_DEVICE = 0, 1
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load():
+    """Load the shared library (built by goldilocks_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        raise ImportError("libgoldilocks_gpu.so is not built (%s): run "
+                          "goldilocks_gb300.build.build() first" % path)
+    lib = ctypes.CDLL(path)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib

@@ -1,0 +1,527 @@
+// C ABI of libgoldilocks_gpu: divisors, plans, transform execution.
+//
+// Reference interfaces (recmo/goldilocks, ntt crate):
+//   gl_is_divisor/gl_split/gl_next/gl_divisors ... ntt/src/divisors.rs:21-89
+//   gl_plan_create (strategy) ..................... ntt/src/ntt/mod.rs:48-78
+//   gl_plan_len / gl_plan_execute (Ntt trait) ..... ntt/src/ntt/mod.rs:25-31
+//   gl_ntt / gl_intt / gl_clear_cache ............. ntt/src/ntt/mod.rs:43-46, 98-120
+//
+// Schedule.  A transform of length n runs as
+//   * one FULL pass (n <= 4096: a CTA holds whole transforms), or
+//   * the four-step pair COL(n1) + ROW(n2), n = n1*n2, both <= 4096: two HBM
+//     passes, the first writing a scratch buffer, the second writing back.
+// The inverse transform is the transform with omega^-1 and the 1/n scale
+// folded into a twiddle table; it equals the reference's intt (scale,
+// reverse values[1..], forward) exactly.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/goldilocks_gpu.h"
+#include "gl_internal.h"
+
+// ------------------------------------------------------------------ status
+
+extern "C" const char *gl_status_string(int status) {
+  switch (status) {
+    case GL_OK: return "ok";
+    case GL_ERR_UNSUPPORTED_SIZE: return "size is not a supported NTT size (does not divide multiplicative order)";
+    case GL_ERR_INVALID: return "invalid argument";
+    case GL_ERR_OOM: return "device out of memory";
+    case GL_ERR_BUDGET: return "request exceeds the HBM admission budget";
+    case GL_ERR_TIMEOUT: return "timed out";
+    case GL_ERR_CUDA: return "CUDA error";
+    case GL_ERR_BUSY: return "queue full";
+    case GL_ERR_CANCELLED: return "cancelled";
+    case GL_ERR_NOT_FOUND: return "unknown request";
+    default: return "unknown status";
+  }
+}
+
+static int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return GL_OK;
+  if (e == cudaErrorMemoryAllocation) return GL_ERR_OOM;
+  return GL_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------- divisors
+
+static const uint64_t kOrder = 0xffffffff00000000ull;  // p - 1
+
+static const std::vector<uint64_t> &divisor_list() {
+  static const std::vector<uint64_t> d = [] {
+    std::vector<uint64_t> v;
+    for (int i = 0; i <= 32; i++) v.push_back(1ull << i);
+    for (uint64_t f : {3ull, 5ull, 17ull, 257ull, 65537ull}) {
+      size_t m = v.size();
+      for (size_t i = 0; i < m; i++) v.push_back(v[i] * f);
+    }
+    std::sort(v.begin(), v.end());
+    return v;
+  }();
+  return d;
+}
+
+extern "C" int gl_is_divisor(uint64_t n) { return n > 0 && kOrder % n == 0; }
+
+extern "C" size_t gl_divisors(uint64_t *out, size_t cap) {
+  const auto &d = divisor_list();
+  if (out)
+    for (size_t i = 0; i < d.size() && i < cap; i++) out[i] = d[i];
+  return d.size();
+}
+
+extern "C" uint64_t gl_next(uint64_t n) {
+  if (n == 0) return 0;
+  const auto &d = divisor_list();
+  auto it = std::lower_bound(d.begin(), d.end(), n);
+  return it == d.end() ? 0 : *it;
+}
+
+extern "C" uint64_t gl_split(uint64_t n) {
+  if (!gl_is_divisor(n)) return 0;
+  const auto &d = divisor_list();
+  uint64_t isqrt = (uint64_t)std::sqrt((double)n);
+  isqrt = (isqrt + n / isqrt) / 2;
+  size_t i = std::lower_bound(d.begin(), d.end(), isqrt) - d.begin();
+  if (i >= d.size()) i = d.size() - 1;
+  for (size_t k = i + 1; k-- > 0;)
+    if (n % d[k] == 0 && n / d[k] >= d[k]) return d[k];
+  return 1;
+}
+
+static uint64_t ugcd(uint64_t a, uint64_t b) {
+  while (b) { uint64_t t = a % b; a = b; b = t; }
+  return a;
+}
+
+// The reference's plan tree for `size` (ntt/src/ntt/mod.rs:60-72), as text.
+static std::string reference_tree(uint64_t size) {
+  if (size <= 128) return "small(" + std::to_string(size) + ")";
+  if (size == 17 || size == 257 || size == 65537)
+    return "Rader(" + std::to_string(size) + ")[" + reference_tree(size - 1) + "]";
+  uint64_t a = gl_split(size), b = size / a;
+  return std::string(ugcd(a, b) == 1 ? "GT(" : "CT(") + std::to_string(a) + "," +
+         std::to_string(b) + ")[" + reference_tree(a) + "," + reference_tree(b) + "]";
+}
+
+// ----------------------------------------------------------- kernel lookup
+
+const gl_kernel_entry *gl_find_kernel(uint64_t m, bool full, bool inv) {
+  size_t cnt = 0;
+  const gl_kernel_entry *e = full ? (inv ? gl_kernels_full_inv(&cnt) : gl_kernels_full_fwd(&cnt))
+                                  : (inv ? gl_kernels_pass_inv(&cnt) : gl_kernels_pass_fwd(&cnt));
+  for (size_t i = 0; i < cnt; i++)
+    if ((uint64_t)e[i].m == m) return &e[i];
+  return nullptr;
+}
+
+// ------------------------------------------------------------------- plans
+
+// Device-resident twiddle tables of one plan on one device.
+struct gl_dev_tables {
+  uint64_t *blk[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [stage][dir] omega_m^e
+  uint64_t *blk_scaled_inv = nullptr;                               // FULL inverse: omega^-e / n
+  uint64_t *tw_lo[2] = {nullptr, nullptr};                          // pass twiddle, [dir]
+  uint64_t *tw_hi[2] = {nullptr, nullptr};
+  std::vector<void *> owned;
+};
+
+struct gl_plan {
+  uint64_t size = 0;
+  int kind = 0;                 // 0: no-op (size <= 1), 1: FULL, 2: COL+ROW
+  uint64_t n1 = 0, n2 = 0;      // kind 2: COL over n1, ROW over n2
+  const gl_kernel_entry *k[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [stage][dir]
+  std::string tree;
+  std::mutex mu;
+  std::map<int, gl_dev_tables> dev;  // per device id
+};
+
+static std::mutex g_cache_mu;
+static std::map<uint64_t, gl_plan *> g_cache;
+
+static uint64_t h_mul(uint64_t a, uint64_t b) { return gl_mul(a, b); }
+
+static uint64_t h_root(uint64_t order, bool inv) {
+  uint64_t w = gl_pow(2717ull, kOrder / order);
+  return inv ? gl_inv(w) : w;
+}
+
+// Pass sizes the COL/ROW kernels are built for.
+static bool pass_size_ok(uint64_t m) { return gl_find_kernel(m, false, false) != nullptr; }
+
+static void choose_schedule(gl_plan *pl) {
+  uint64_t n = pl->size;
+  if (n <= 1) { pl->kind = 0; return; }
+  if (gl_find_kernel(n, true, false)) {
+    pl->kind = 1;
+    for (int d = 0; d < 2; d++) pl->k[0][d] = gl_find_kernel(n, true, d == 1);
+    return;
+  }
+  // Four-step: prefer n1 <= n2 nearest sqrt(n), both with pass kernels.
+  uint64_t best1 = 0;
+  for (uint64_t n1 : divisor_list()) {
+    if (n1 > n) break;
+    if (n % n1) continue;
+    uint64_t n2 = n / n1;
+    if (!pass_size_ok(n1) || !pass_size_ok(n2)) continue;
+    if (n1 % GL_PASS_LANES || n2 % GL_PASS_LANES) continue;
+    if (best1 == 0 || (std::max(n1, n2) < std::max(best1, n / best1)) ||
+        (std::max(n1, n2) == std::max(best1, n / best1) && n1 > best1))
+      best1 = n1;
+  }
+  if (best1) {
+    pl->kind = 2;
+    pl->n1 = best1;
+    pl->n2 = n / best1;
+    for (int d = 0; d < 2; d++) {
+      pl->k[0][d] = gl_find_kernel(pl->n1, false, d == 1);
+      pl->k[1][d] = gl_find_kernel(pl->n2, false, d == 1);
+    }
+    return;
+  }
+  pl->kind = -1;  // divisor without a GPU schedule
+}
+
+static int upload(gl_dev_tables &t, const std::vector<uint64_t> &h, uint64_t **dst) {
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, h.size() * sizeof(uint64_t));
+  if (e != cudaSuccess) return cuda_status(e);
+  e = cudaMemcpy(p, h.data(), h.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { cudaFree(p); return cuda_status(e); }
+  t.owned.push_back(p);
+  *dst = (uint64_t *)p;
+  return GL_OK;
+}
+
+static std::vector<uint64_t> powers(uint64_t w, uint64_t count, uint64_t scale) {
+  std::vector<uint64_t> v(count);
+  uint64_t x = scale;
+  for (uint64_t i = 0; i < count; i++) { v[i] = x; x = h_mul(x, w); }
+  return v;
+}
+
+// Twiddle tables for the current device, built on first use.
+static int plan_tables(gl_plan *pl, gl_dev_tables **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e);
+  std::lock_guard<std::mutex> lk(pl->mu);
+  auto it = pl->dev.find(dev);
+  if (it != pl->dev.end()) { *out = &it->second; return GL_OK; }
+  gl_dev_tables t;
+  int st = GL_OK;
+  const uint64_t n = pl->size;
+  if (pl->kind == 1) {
+    for (int d = 0; d < 2 && st == GL_OK; d++)
+      st = upload(t, powers(h_root(n, d), n, 1), &t.blk[0][d]);
+    if (st == GL_OK) st = upload(t, powers(h_root(n, true), n, gl_inv(n % GL_P)), &t.blk_scaled_inv);
+  } else if (pl->kind == 2) {
+    const uint64_t hi_count = (n + GL_TW_SPLIT - 1) / GL_TW_SPLIT;
+    for (int d = 0; d < 2 && st == GL_OK; d++) {
+      st = upload(t, powers(h_root(pl->n1, d), pl->n1, 1), &t.blk[0][d]);
+      if (st == GL_OK) st = upload(t, powers(h_root(pl->n2, d), pl->n2, 1), &t.blk[1][d]);
+      const uint64_t w = h_root(n, d);
+      const uint64_t scale = d ? gl_inv(n % GL_P) : 1;
+      if (st == GL_OK) st = upload(t, powers(w, GL_TW_SPLIT, scale), &t.tw_lo[d]);
+      if (st == GL_OK) st = upload(t, powers(gl_pow(w, GL_TW_SPLIT), hi_count, 1), &t.tw_hi[d]);
+    }
+  }
+  if (st != GL_OK) {
+    for (void *p : t.owned) cudaFree(p);
+    return st;
+  }
+  auto res = pl->dev.emplace(dev, std::move(t));
+  *out = &res.first->second;
+  return GL_OK;
+}
+
+extern "C" int gl_plan_create(uint64_t size, gl_plan **out) {
+  if (!out) return GL_ERR_INVALID;
+  *out = nullptr;
+  if (!gl_is_divisor(size)) return GL_ERR_UNSUPPORTED_SIZE;
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  auto it = g_cache.find(size);
+  if (it != g_cache.end()) { *out = it->second; return GL_OK; }
+  gl_plan *pl = new gl_plan();
+  pl->size = size;
+  pl->tree = reference_tree(size);
+  choose_schedule(pl);
+  if (pl->kind < 0) {
+    delete pl;
+    return GL_ERR_UNSUPPORTED_SIZE;
+  }
+  g_cache[size] = pl;
+  *out = pl;
+  return GL_OK;
+}
+
+// Plans are shared and immutable once built; a cleared cache forgets them
+// but keeps them alive so that handles held by callers stay valid.
+extern "C" void gl_plan_release(gl_plan *) {}
+
+extern "C" void gl_clear_cache(void) {
+  static std::vector<gl_plan *> retired;
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  for (auto &kv : g_cache) retired.push_back(kv.second);
+  g_cache.clear();
+}
+
+extern "C" uint64_t gl_plan_len(const gl_plan *plan) { return plan ? plan->size : 0; }
+
+extern "C" int gl_plan_describe(const gl_plan *plan, char *buf, size_t cap) {
+  if (!plan || !buf) return GL_ERR_INVALID;
+  std::string s = plan->tree + " | gpu: ";
+  auto kname = [](const gl_kernel_entry *k) {
+    return std::to_string(k->m) + " (" + std::to_string(k->ma) + "x" + std::to_string(k->mb) + ")";
+  };
+  if (plan->kind == 0) s += "no-op";
+  else if (plan->kind == 1) s += "full " + kname(plan->k[0][0]);
+  else s += "col " + kname(plan->k[0][0]) + " + row " + kname(plan->k[1][0]);
+  size_t n = std::min(cap - 1, s.size());
+  memcpy(buf, s.data(), n);
+  buf[n] = 0;
+  return s.size() < cap ? GL_OK : GL_ERR_INVALID;
+}
+
+extern "C" uint64_t gl_plan_workspace_bytes(const gl_plan *plan, uint64_t count) {
+  if (!plan || plan->kind != 2) return 0;
+  return plan->size * count * sizeof(uint64_t);
+}
+
+// ---------------------------------------------------------------- profiling
+
+struct gl_prof_rec {
+  const gl_kernel_entry *k;
+  int col;  // role: 0 full, 1 col, 2 row
+  uint64_t elements;
+  cudaEvent_t a, b;
+};
+static std::mutex g_prof_mu;
+static bool g_prof_on = false;
+static std::vector<gl_prof_rec> g_prof;
+
+static std::string kernel_label(const gl_kernel_entry *k, int role) {
+  static const char *roles[] = {"full", "col", "row"};
+  return std::string(roles[role]) + " " + std::to_string(k->m) + " (" + std::to_string(k->ma) +
+         "x" + std::to_string(k->mb) + ")";
+}
+
+// Launch `k` with optional event bracketing.  role: 0 full, 1 col, 2 row.
+static void launch(const gl_kernel_entry *k, int role, const gl_pass_args &a, dim3 grid,
+                   uint64_t elements, cudaStream_t stream) {
+  bool on;
+  { std::lock_guard<std::mutex> lk(g_prof_mu); on = g_prof_on; }
+  if (!on) { k->launch(a, grid, stream); return; }
+  gl_prof_rec r{k, role, elements, nullptr, nullptr};
+  cudaEventCreate(&r.a);
+  cudaEventCreate(&r.b);
+  cudaEventRecord(r.a, stream);
+  k->launch(a, grid, stream);
+  cudaEventRecord(r.b, stream);
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof.push_back(r);
+}
+
+extern "C" int gl_profile_enable(int on) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  for (auto &r : g_prof) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+  g_prof.clear();
+  g_prof_on = on != 0;
+  return GL_OK;
+}
+
+extern "C" int gl_profile_read(gl_profile_entry *out, int cap) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  std::map<std::string, gl_profile_entry> agg;
+  for (auto &r : g_prof) {
+    cudaError_t e = cudaEventSynchronize(r.b);
+    if (e != cudaSuccess) return -cuda_status(e);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    std::string name = kernel_label(r.k, (int)r.col);
+    gl_profile_entry &en = agg[name];
+    snprintf(en.name, sizeof(en.name), "%s", name.c_str());
+    en.launches += 1;
+    en.elements += r.elements;
+    en.total_ms += ms;
+  }
+  int i = 0;
+  for (auto &kv : agg) {
+    if (out && i < cap) out[i] = kv.second;
+    i++;
+  }
+  return i;
+}
+
+// ---------------------------------------------------------------- execution
+
+static const uint32_t kMaxGridY = 65535;
+
+// Queue the transform of `count` contiguous transforms at device pointer
+// `data` on `stream`, using `scratch` (>= size*count words) for kind 2.
+static int run_device(gl_plan *pl, uint64_t *data, uint64_t count, bool inv, uint64_t *scratch,
+                      cudaStream_t stream) {
+  if (pl->kind == 0 || count == 0) return GL_OK;
+  gl_dev_tables *t = nullptr;
+  int st = plan_tables(pl, &t);
+  if (st != GL_OK) return st;
+  const int d = inv ? 1 : 0;
+  const uint64_t n = pl->size;
+  if (pl->kind == 1) {
+    const gl_kernel_entry *k = pl->k[0][d];
+    gl_pass_args a{};
+    a.in = data; a.out = data;
+    a.in_ls = (int64_t)n; a.in_is = 1; a.out_ls = (int64_t)n; a.out_is = 1;
+    a.in_bs = 0; a.out_bs = 0;
+    a.flags = 0;
+    a.tw_m = inv ? t->blk_scaled_inv : t->blk[0][0];
+    if (inv) a.flags |= GL_PF_SCALE_ALL;
+    // Lanes are batch items; split very large batches across launches.
+    const uint64_t per_launch = (uint64_t)k->lanes * 0x7fffffffull;
+    for (uint64_t off = 0; off < count; off += per_launch) {
+      uint64_t c = std::min(per_launch, count - off);
+      a.in = data + off * n; a.out = data + off * n;
+      a.lanes = (uint32_t)c;
+      dim3 grid((unsigned)((c + k->lanes - 1) / k->lanes), 1);
+      launch(k, 0, a, grid, c * n, stream);
+    }
+  } else {
+    const uint64_t n1 = pl->n1, n2 = pl->n2;
+    const gl_kernel_entry *kc = pl->k[0][d], *kr = pl->k[1][d];
+    for (uint64_t off = 0; off < count; off += kMaxGridY) {
+      const uint64_t c = std::min<uint64_t>(kMaxGridY, count - off);
+      gl_pass_args a{};  // COL: data -> scratch
+      a.in = data + off * n; a.out = scratch + off * n;
+      a.in_ls = 1; a.in_is = (int64_t)n2; a.out_ls = 1; a.out_is = (int64_t)n2;
+      a.in_bs = (int64_t)n; a.out_bs = (int64_t)n;
+      a.lanes = (uint32_t)n2;
+      a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
+      a.tw_m = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
+      launch(kc, 1, a, dim3((unsigned)(n2 / GL_PASS_LANES), (unsigned)c), c * n, stream);
+      gl_pass_args b{};  // ROW: scratch -> data (transposed store)
+      b.in = scratch + off * n; b.out = data + off * n;
+      b.in_ls = (int64_t)n2; b.in_is = 1; b.out_ls = 1; b.out_is = (int64_t)n1;
+      b.in_bs = (int64_t)n; b.out_bs = (int64_t)n;
+      b.lanes = (uint32_t)n1;
+      b.flags = GL_PF_STORE_LANE_FAST;
+      b.tw_m = t->blk[1][d];
+      launch(kr, 2, b, dim3((unsigned)(n1 / GL_PASS_LANES), (unsigned)c), c * n, stream);
+    }
+  }
+  return cuda_status(cudaGetLastError());
+}
+
+static void init_mempool_once() {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;  // keep freed blocks cached in this process
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  });
+}
+
+static int execute(gl_plan *pl, uint64_t *data, uint64_t len, int dir, int mem, void *ws,
+                   uint64_t ws_bytes, cudaStream_t stream) {
+  if (!pl || (!data && len)) return GL_ERR_INVALID;
+  if (dir != GL_FORWARD && dir != GL_INVERSE) return GL_ERR_INVALID;
+  if (mem != GL_MEM_HOST && mem != GL_MEM_DEVICE) return GL_ERR_INVALID;
+  if (len == 0) return GL_OK;
+  if (pl->size == 0 || len % pl->size) return GL_ERR_INVALID;
+  const uint64_t count = len / pl->size;
+  const bool inv = dir == GL_INVERSE;
+  if (pl->kind == 0) return GL_OK;
+  init_mempool_once();
+  const uint64_t need = gl_plan_workspace_bytes(pl, count);
+  int st = GL_OK;
+  if (mem == GL_MEM_DEVICE) {
+    uint64_t *scratch = (uint64_t *)ws;
+    bool own = false;
+    if (need && (!ws || ws_bytes < need)) {
+      if (ws) return GL_ERR_INVALID;
+      cudaError_t e = cudaMallocAsync((void **)&scratch, need, stream);
+      if (e != cudaSuccess) return cuda_status(e);
+      own = true;
+    }
+    st = run_device(pl, data, count, inv, scratch, stream);
+    if (own) cudaFreeAsync(scratch, stream);
+    return st;
+  }
+  // Host memory: stage through the device and return when the result is back.
+  uint64_t *dbuf = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&dbuf, len * sizeof(uint64_t) + need, stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  e = cudaMemcpyAsync(dbuf, data, len * sizeof(uint64_t), cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess) {
+    st = run_device(pl, dbuf, count, inv, need ? dbuf + len : nullptr, stream);
+    if (st == GL_OK)
+      e = cudaMemcpyAsync(data, dbuf, len * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream);
+  }
+  cudaFreeAsync(dbuf, stream);
+  cudaError_t e2 = cudaStreamSynchronize(stream);
+  if (st != GL_OK) return st;
+  if (e != cudaSuccess) return cuda_status(e);
+  return cuda_status(e2);
+}
+
+extern "C" int gl_plan_execute(const gl_plan *plan, uint64_t *data, uint64_t len, int dir, int mem,
+                               void *stream) {
+  return execute(const_cast<gl_plan *>(plan), data, len, dir, mem, nullptr, 0,
+                 (cudaStream_t)stream);
+}
+
+extern "C" int gl_plan_execute_ws(const gl_plan *plan, uint64_t *data, uint64_t len, int dir,
+                                  void *workspace, uint64_t workspace_bytes, void *stream) {
+  if (!workspace && gl_plan_workspace_bytes(plan, plan && plan->size ? len / plan->size : 0))
+    return GL_ERR_INVALID;
+  return execute(const_cast<gl_plan *>(plan), data, len, dir, GL_MEM_DEVICE, workspace,
+                 workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int gl_ntt(uint64_t *values, uint64_t len, int mem, void *stream) {
+  gl_plan *pl = nullptr;
+  int st = gl_plan_create(len, &pl);  // len 0 is not a divisor: the reference panics too
+  if (st != GL_OK) return st;
+  return gl_plan_execute(pl, values, len, GL_FORWARD, mem, stream);
+}
+
+extern "C" int gl_intt(uint64_t *values, uint64_t len, int mem, void *stream) {
+  if (len <= 1) return GL_OK;  // ntt/mod.rs:105-107
+  gl_plan *pl = nullptr;
+  int st = gl_plan_create(len, &pl);
+  if (st != GL_OK) return st;
+  return gl_plan_execute(pl, values, len, GL_INVERSE, mem, stream);
+}
+
+// ------------------------------------------------------------------ inputs
+
+static inline uint64_t splitmix64(uint64_t x) {
+  uint64_t z = x + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+extern "C" void gl_fill_uniform(uint64_t *out, uint64_t n, uint64_t seed, uint64_t offset) {
+  const uint64_t s = splitmix64(seed);
+  for (uint64_t i = 0; i < n; i++) {
+    uint64_t v;
+    for (uint64_t k = 0;; k++) {
+      v = splitmix64(s ^ (offset + i + (k << 48)));
+      if (v < GL_P) break;
+    }
+    out[i] = v;
+  }
+}

@@ -1,0 +1,144 @@
+"""Python mirror of the reference's `goldilocks_ntt::ntt` interface.
+
+Reference (recmo/goldilocks, ntt crate):
+  strategy(size) -> Arc<dyn Ntt> ......... ntt/src/ntt/mod.rs:48-78   -> strategy()/Plan
+  Ntt::len / Ntt::ntt .................... ntt/src/ntt/mod.rs:25-31   -> Plan.len()/Plan.ntt()
+  ntt(values) / intt(values) ............. ntt/src/ntt/mod.rs:98-120  -> ntt()/intt()
+  clear_cache() .......................... ntt/src/ntt/mod.rs:43-46
+  divisors / is_divisor / split / next ... ntt/src/divisors.rs:21-89
+
+`values` is either a host numpy array of dtype uint64 (C-contiguous; the call
+stages it through the GPU and returns when the result is back, like the
+reference), or a CUDA torch tensor of dtype int64/uint64 (the work is queued on
+the tensor's current stream).  Unsupported sizes raise ValueError with the
+reference's panic message.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+
+MODULUS = 0xFFFF_FFFF_0000_0001
+
+
+class GoldilocksError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        msg = L.load().gl_status_string(status).decode()
+        super().__init__("%s%s (status %d)" % (what + ": " if what else "", msg, status))
+
+
+def _check(status, what="", size=None):
+    if status == L.GL_OK:
+        return
+    if status == L.GL_ERR_UNSUPPORTED_SIZE and size is not None:
+        raise ValueError("%d is not a supported NTT size (does not divide multiplicative order)" % size)
+    raise GoldilocksError(status, what)
+
+
+def _buffer(values):
+    """(pointer, length, mem, stream) for a numpy array or CUDA tensor."""
+    if isinstance(values, np.ndarray):
+        if values.dtype != np.uint64:
+            raise TypeError("host values must be a numpy uint64 array")
+        if not values.flags.c_contiguous or not values.flags.writeable:
+            raise ValueError("host values must be C-contiguous and writeable")
+        return values.ctypes.data, values.size, L.GL_MEM_HOST, None
+    try:
+        import torch
+    except ImportError:  # pragma: no cover
+        torch = None
+    if torch is not None and isinstance(values, torch.Tensor):
+        if not values.is_cuda:
+            raise ValueError("torch tensors must live on a CUDA device (use numpy for host data)")
+        if values.element_size() != 8 or values.dtype.is_floating_point:
+            raise TypeError("device values must be a 64-bit integer tensor")
+        if not values.is_contiguous():
+            raise ValueError("device values must be contiguous")
+        stream = torch.cuda.current_stream(values.device).cuda_stream
+        return values.data_ptr(), values.numel(), L.GL_MEM_DEVICE, stream
+    raise TypeError("values must be a numpy uint64 array or a CUDA torch tensor")
+
+
+def is_divisor(n):
+    return bool(L.load().gl_is_divisor(n))
+
+
+def split(n):
+    if not is_divisor(n):
+        raise ValueError("%d does not divide multiplicative group order." % n)
+    return int(L.load().gl_split(n))
+
+
+def next(n):  # noqa: A001 -- the reference's name (divisors::next)
+    return int(L.load().gl_next(n))
+
+
+def divisors():
+    buf = (ctypes.c_uint64 * 1056)()
+    n = L.load().gl_divisors(buf, 1056)
+    return [int(x) for x in buf[:n]]
+
+
+class Plan:
+    """A cached transform plan for one size (the reference's `Arc<dyn Ntt>`)."""
+
+    def __init__(self, size):
+        h = ctypes.c_void_p()
+        _check(L.load().gl_plan_create(size, ctypes.byref(h)), "plan", size=size)
+        self._h = h
+        self.size = size
+
+    def len(self):
+        return int(L.load().gl_plan_len(self._h))
+
+    def describe(self):
+        buf = ctypes.create_string_buffer(1 << 16)
+        L.load().gl_plan_describe(self._h, buf, len(buf))
+        return buf.value.decode()
+
+    def workspace_bytes(self, count=1):
+        return int(L.load().gl_plan_workspace_bytes(self._h, count))
+
+    def _run(self, values, direction):
+        ptr, n, mem, stream = _buffer(values)
+        if n % self.size:
+            raise ValueError("length %d is not a multiple of the plan size %d" % (n, self.size))
+        _check(L.load().gl_plan_execute(self._h, ptr, n, direction, mem, stream), "execute")
+        return values
+
+    def ntt(self, values):
+        """Forward transforms of len(values)/size contiguous blocks, in place."""
+        return self._run(values, L.GL_FORWARD)
+
+    def intt(self, values):
+        """Inverse transforms (1/n scaled) of contiguous blocks, in place."""
+        return self._run(values, L.GL_INVERSE)
+
+
+def strategy(size):
+    return Plan(size)
+
+
+def ntt(values):
+    ptr, n, mem, stream = _buffer(values)
+    _check(L.load().gl_ntt(ptr, n, mem, stream), "ntt", size=n)
+    return values
+
+
+def intt(values):
+    ptr, n, mem, stream = _buffer(values)
+    _check(L.load().gl_intt(ptr, n, mem, stream), "intt", size=n)
+    return values
+
+
+def clear_cache():
+    L.load().gl_clear_cache()
+
+
+def fill_uniform(n, seed, offset=0):
+    """Seeded field elements uniform in [0, p) (see gl_fill_uniform)."""
+    out = np.empty(n, dtype=np.uint64)
+    L.load().gl_fill_uniform(out.ctypes.data, n, seed, offset)
+    return out

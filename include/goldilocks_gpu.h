@@ -1,0 +1,129 @@
+/* goldilocks_gpu.h -- C ABI of the GB300 (sm_103a) Goldilocks NTT library.
+ *
+ * Drop-in boundary for the transform path of recmo/goldilocks' `goldilocks-ntt`
+ * crate: the functions below are what that crate's `Ntt` slot (the `gpu`
+ * feature, ntt/src/ntt/gpu/mod.rs:153-209) or any FFI caller binds.  Only plain
+ * pointers, sizes and integers cross the boundary.
+ *
+ * Field elements are u64 words.  The library works on either representation
+ * the caller uses -- canonical values in [0, p) or the reference's Montgomery
+ * words x*2^64 mod p (ntt/src/field/mod.rs:12) -- because every operation on
+ * the path is F_p-linear.  Outputs are fully reduced (< p).  Inputs >= p are
+ * accepted and treated as their residue mod p.
+ *
+ * Memory: `mem` says where `data` lives.  GL_MEM_HOST: the call copies to the
+ * GPU, runs, copies back and returns when the result is in `data`
+ * (synchronous, like the reference).  GL_MEM_DEVICE: `data` is device memory;
+ * the work is queued on `stream` (a cudaStream_t, NULL = legacy default
+ * stream) and the call returns without waiting.
+ *
+ * Errors: every call returns a gl_status.  The reference panics on an
+ * unsupported size ("{size} is not a supported NTT size (does not divide
+ * multiplicative order)", ntt/src/ntt/mod.rs:55-58); here that is
+ * GL_ERR_UNSUPPORTED_SIZE and nothing is modified.
+ *
+ * Threading: all functions are thread-safe; plans are cached under a mutex
+ * and shared (ntt/src/ntt/mod.rs:23).
+ */
+#ifndef GOLDILOCKS_GPU_H
+#define GOLDILOCKS_GPU_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GL_OK = 0,
+  GL_ERR_UNSUPPORTED_SIZE = 1, /* size does not divide p - 1 (reference: panic) */
+  GL_ERR_INVALID = 2,          /* null pointer, len % size != 0, bad enum */
+  GL_ERR_OOM = 3,              /* device allocation failed */
+  GL_ERR_BUDGET = 4,           /* request exceeds the server's HBM budget */
+  GL_ERR_TIMEOUT = 5,          /* a bounded wait expired */
+  GL_ERR_CUDA = 6,             /* a CUDA runtime call failed */
+  GL_ERR_BUSY = 7,             /* queue full; retry later */
+  GL_ERR_CANCELLED = 8,        /* request cancelled before it ran */
+  GL_ERR_NOT_FOUND = 9         /* unknown request id */
+} gl_status;
+
+enum { GL_FORWARD = 0, GL_INVERSE = 1 };
+enum { GL_MEM_HOST = 0, GL_MEM_DEVICE = 1 };
+
+typedef struct gl_plan gl_plan;
+
+/* Human-readable name of a status code. */
+const char *gl_status_string(int status);
+
+/* ---- number theory (ntt/src/divisors.rs) ---- */
+
+/* divisors.rs:21-23: n > 0 and n divides p - 1. */
+int gl_is_divisor(uint64_t n);
+/* divisors.rs:67-89: the split a <= b, a*b = n, a nearest sqrt(n); 0 if n is
+ * not a divisor. */
+uint64_t gl_split(uint64_t n);
+/* divisors.rs:52-59: smallest divisor >= n (0 for 0 or beyond p - 1). */
+uint64_t gl_next(uint64_t n);
+/* divisors.rs:32-47: writes min(cap, 1056) sorted divisors, returns 1056. */
+size_t gl_divisors(uint64_t *out, size_t cap);
+
+/* ---- plans (ntt/src/ntt/mod.rs:25-96) ---- */
+
+/* strategy(size), mod.rs:48-78: look up or build the cached plan for `size`.
+ * The returned handle is shared; gl_plan_release is optional. */
+int gl_plan_create(uint64_t size, gl_plan **out);
+void gl_plan_release(gl_plan *plan);
+/* Ntt::len, mod.rs:26. */
+uint64_t gl_plan_len(const gl_plan *plan);
+/* The reference's plan tree for this size (e.g. "CT(4096,4096)[CT(64,64)[...]]")
+ * followed by the GPU schedule ("| gpu: col 4096 (64x64) + row 4096 (64x64)").
+ * Returns GL_OK, or GL_ERR_INVALID if `cap` is too small (output truncated). */
+int gl_plan_describe(const gl_plan *plan, char *buf, size_t cap);
+/* Bytes of device scratch gl_plan_execute_ws needs for `count` transforms. */
+uint64_t gl_plan_workspace_bytes(const gl_plan *plan, uint64_t count);
+/* Ntt::ntt, mod.rs:30: `len` must be a multiple of the plan length; the
+ * len/size contiguous transforms are done in place.  dir = GL_FORWARD runs
+ * the reference's ntt; GL_INVERSE its intt (mod.rs:104-120: scale by 1/n,
+ * reverse values[1..], forward -- computed here as the transform with
+ * omega^-1 and the 1/n scale folded into a twiddle table). */
+int gl_plan_execute(const gl_plan *plan, uint64_t *data, uint64_t len, int dir, int mem,
+                    void *stream);
+/* As gl_plan_execute with GL_MEM_DEVICE, using caller-provided device scratch
+ * of at least gl_plan_workspace_bytes(plan, len / size) bytes. */
+int gl_plan_execute_ws(const gl_plan *plan, uint64_t *data, uint64_t len, int dir,
+                       void *workspace, uint64_t workspace_bytes, void *stream);
+
+/* ---- free functions (ntt/src/ntt/mod.rs:43-46, 98-120) ---- */
+
+/* ntt::ntt: forward transform of `values` (length len) in place. */
+int gl_ntt(uint64_t *values, uint64_t len, int mem, void *stream);
+/* ntt::intt: inverse transform in place (lengths 0 and 1 are no-ops). */
+int gl_intt(uint64_t *values, uint64_t len, int mem, void *stream);
+/* ntt::clear_cache: forget cached plans (handles already returned stay valid). */
+void gl_clear_cache(void);
+
+/* Fill out[0..n) with field elements uniform in [0, p): element i is the
+ * first of splitmix64(splitmix64(seed) ^ (offset + i + (k << 48))), k = 0, 1,
+ * ..., that is below p.  Host memory; the bench and tests use it for seeded
+ * synthetic inputs. */
+void gl_fill_uniform(uint64_t *out, uint64_t n, uint64_t seed, uint64_t offset);
+
+/* ---- kernel timing for benchmarks (no counterpart in the reference) ---- */
+
+typedef struct {
+  char name[48];       /* kernel role and shape, e.g. "col 4096 (64x64)" */
+  uint64_t launches;   /* launches recorded */
+  uint64_t elements;   /* field elements read (and written) by those launches */
+  double total_ms;     /* summed CUDA-event duration */
+} gl_profile_entry;
+
+/* While enabled, every kernel launch of the library is bracketed by CUDA
+ * events on its own stream.  Enabling clears previous records. */
+int gl_profile_enable(int on);
+/* Synchronises the recorded events and aggregates them by kernel; writes up
+ * to `cap` entries and returns how many exist (or a negative gl_status). */
+int gl_profile_read(gl_profile_entry *out, int cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,135 @@
+"""CPU oracle for the Goldilocks NTT path -- TEST INFRASTRUCTURE ONLY.
+
+A C restatement of recmo/goldilocks' `goldilocks-ntt` transform path
+(gl_oracle.c, codelets_gen.c from codegen_ref.py), loaded through ctypes.
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it,
+as the checker; the product (goldilocks_gb300/) never does.
+
+Parity is pinned by the reference's own artefacts (tests/golden/): the 860
+codelet constants of ntt/src/ntt/small.rs, the known-answer tests of the
+reference's unit tests, and O(n^2) DFT vectors.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libgl_oracle.so")
+SOURCES = [os.path.join(HERE, "gl_oracle.c"), os.path.join(HERE, "codelets_gen.c")]
+P = 0xFFFF_FFFF_0000_0001
+
+
+def build():
+    """Compile the oracle with gcc (incremental)."""
+    os.makedirs(BUILD, exist_ok=True)
+    deps = SOURCES + [os.path.join(HERE, "gl_oracle.h"), os.path.join(HERE, "gl_oracle_internal.h")]
+    if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
+        return LIB
+    objs = []
+    procs = []
+    for src in SOURCES:
+        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        objs.append(obj)
+        procs.append(subprocess.Popen(["gcc", "-O2", "-fPIC", "-std=c11", "-c", src, "-o", obj],
+                                      stderr=subprocess.PIPE, text=True))
+    for p in procs:
+        _, err = p.communicate()
+        if p.returncode:
+            raise RuntimeError("oracle build failed:\n" + err)
+    tmp = LIB + ".tmp"
+    subprocess.run(["gcc", "-shared", "-o", tmp] + objs + ["-lm", "-lpthread"], check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+_u64 = ctypes.c_uint64
+_vp = ctypes.c_void_p
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        l = ctypes.CDLL(LIB)
+        for f in ("glo_add", "glo_sub", "glo_mul", "glo_shift", "glo_root_384", "glo_pow"):
+            getattr(l, f).restype = _u64
+            getattr(l, f).argtypes = [_u64, _u64]
+        for f in ("glo_inv", "glo_root", "glo_split", "glo_next", "glo_to_mont", "glo_from_mont"):
+            getattr(l, f).restype = _u64
+            getattr(l, f).argtypes = [_u64]
+        l.glo_is_divisor.argtypes = [_u64]
+        l.glo_divisors.restype = ctypes.c_size_t
+        l.glo_divisors.argtypes = [_vp, ctypes.c_size_t]
+        for f in ("glo_naive_ntt", "glo_naive_intt"):
+            getattr(l, f).argtypes = [_vp, ctypes.c_size_t]
+        l.glo_ntt_batch.argtypes = [_vp, ctypes.c_size_t, ctypes.c_size_t]
+        l.glo_ntt.argtypes = [_vp, ctypes.c_size_t]
+        l.glo_intt.argtypes = [_vp, ctypes.c_size_t]
+        l.glo_strategy_describe.argtypes = [_u64, ctypes.c_char_p, ctypes.c_size_t]
+        l.glo_coset_lde.argtypes = [_vp, _vp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_uint32, _u64]
+        l.glo_convolve.argtypes = [_vp, _vp, ctypes.c_size_t]
+        _lib = l
+    return _lib
+
+
+def _arr(x):
+    x = np.ascontiguousarray(x, dtype=np.uint64)
+    return x
+
+
+def ntt(x, size=None):
+    """Forward transform(s); `size` splits x into len(x)/size contiguous transforms."""
+    y = _arr(x).copy()
+    n = y.size
+    rc = lib().glo_ntt_batch(y.ctypes.data, n, size if size is not None else n) if n else 0
+    if rc:
+        raise ValueError("oracle: unsupported size")
+    return y
+
+
+def intt(x, size=None):
+    y = _arr(x).copy()
+    size = size if size is not None else y.size
+    for off in range(0, y.size, max(size, 1)):
+        seg = y[off:off + size]
+        if lib().glo_intt(seg.ctypes.data, size):
+            raise ValueError("oracle: unsupported size")
+    return y
+
+
+def naive_ntt(x):
+    y = _arr(x).copy()
+    lib().glo_naive_ntt(y.ctypes.data, y.size)
+    return y
+
+
+def naive_intt(x):
+    y = _arr(x).copy()
+    lib().glo_naive_intt(y.ctypes.data, y.size)
+    return y
+
+
+def coset_lde(x, n, cols, blowup, shift):
+    x = _arr(x)
+    out = np.empty(n * blowup * cols, dtype=np.uint64)
+    if lib().glo_coset_lde(x.ctypes.data, out.ctypes.data, n, cols, blowup, shift):
+        raise ValueError("oracle: unsupported LDE shape")
+    return out
+
+
+def strategy_describe(size):
+    buf = ctypes.create_string_buffer(1 << 16)
+    if lib().glo_strategy_describe(size, buf, len(buf)):
+        raise ValueError("oracle: unsupported size")
+    return buf.value.decode()
+
+
+def divisors():
+    buf = (ctypes.c_uint64 * 1056)()
+    lib().glo_divisors(ctypes.addressof(buf), 1056)
+    return [int(v) for v in buf]
