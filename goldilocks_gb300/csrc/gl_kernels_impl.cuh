@@ -8,11 +8,8 @@ template <int MA, int MB, int LANES, bool INV>
 static void gl_launch_pass(const gl_pass_args &args, dim3 grid, cudaStream_t stream) {
   constexpr size_t smem = gl_pass_smem_bytes<MA, MB>(LANES);
   auto kern = gl_pass_kernel<MA, MB, LANES, INV>;
-  static bool attr_done = false;  // idempotent; a racing second set is harmless
-  if (!attr_done && smem > 48 * 1024) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr_done = true;
-  }
+  // The opt-in is per device context; setting it again is cheap and idempotent.
+  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   kern<<<grid, LANES * MB, smem, stream>>>(args);
 }
 
