@@ -33,6 +33,8 @@ SIGNATURES = [
     ("gl_intt", _int, [_vp, _u64, _int, _vp]),
     ("gl_clear_cache", None, []),
     ("gl_fill_uniform", None, [_vp, _u64, _u64, _u64]),
+    ("gl_ntt_columns", _int, [_vp, _u64, _u64, _int, _int, _vp]),
+    ("gl_coset_lde", _int, [_vp, _vp, _u64, _u64, _u32, _u64, _int, _vp]),
     ("gl_profile_enable", _int, [_int]),
     ("gl_profile_read", _int, [_vp, _int]),
 ]

@@ -1,0 +1,85 @@
+"""Command-line timing of single transforms, after the reference's bench binary
+(bench/src/main.rs:111-189: sweep sizes, print `size,duration,throughput`).
+
+  python -m goldilocks_gb300.cli --sizes 16777216 --reps 3     # one size
+  python -m goldilocks_gb300.cli --max-exponent 24             # smooth divisors
+  python -m goldilocks_gb300.cli --sizes 1048576 --cols 256 --lde 4
+
+Inputs are device-resident; durations are CUDA-event medians (seconds).
+"""
+import argparse
+import statistics
+import sys
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--sizes", type=str, default="", help="comma-separated sizes")
+    ap.add_argument("--max-exponent", type=int, default=20)
+    ap.add_argument("--all", action="store_true", help="all divisors, not only smooth ones")
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--inverse", action="store_true")
+    ap.add_argument("--cols", type=int, default=1, help="transform the columns of a rows x cols matrix")
+    ap.add_argument("--lde", type=int, default=0, help="coset LDE with this blowup (shift 7)")
+    args = ap.parse_args(argv)
+
+    import numpy as np
+    import torch
+
+    import goldilocks_gb300 as gl
+    from goldilocks_gb300 import _lib as L
+
+    lib = L.load()
+    if args.sizes:
+        sizes = [int(s) for s in args.sizes.split(",")]
+    else:
+        smooth = 64424509440  # 2^32 * 3 * 5: divisors without 17, 257, 65537
+        sizes = [d for d in gl.divisors() if 2 <= d <= (1 << args.max_exponent)
+                 and (args.all or smooth % d == 0 or d % 17 == 0 and smooth * 17 % d == 0)]
+    stream = torch.cuda.current_stream()
+    print("size,cols,duration,throughput")
+    for n in sizes:
+        x = gl.fill_uniform(n * args.cols, seed=n)
+        d = torch.from_numpy(x.view(np.int64)).cuda()
+        out = None
+        if args.lde:
+            out = torch.empty(n * args.cols * args.lde, dtype=torch.int64, device="cuda")
+
+        def run():
+            if args.lde:
+                rc = lib.gl_coset_lde(d.data_ptr(), out.data_ptr(), n, args.cols, args.lde, 7,
+                                      L.GL_MEM_DEVICE, stream.cuda_stream)
+            elif args.cols > 1:
+                rc = lib.gl_ntt_columns(d.data_ptr(), n, args.cols,
+                                        L.GL_INVERSE if args.inverse else L.GL_FORWARD,
+                                        L.GL_MEM_DEVICE, stream.cuda_stream)
+            else:
+                pl = gl.strategy(n)
+                (pl.intt if args.inverse else pl.ntt)(d)
+                rc = 0
+            if rc:
+                raise gl.GoldilocksError(rc, "cli")
+
+        try:
+            for _ in range(args.warmup):
+                run()
+            times = []
+            for _ in range(args.reps):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                run()
+                b.record(stream)
+                b.synchronize()
+                times.append(a.elapsed_time(b) * 1e-3)
+        except ValueError as e:
+            print("%d,%d,unsupported,%s" % (n, args.cols, e), file=sys.stderr)
+            continue
+        t = statistics.median(times)
+        print("%d,%d,%.9f,%.6e" % (n, args.cols, t, n * args.cols / t))
+        sys.stdout.flush()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

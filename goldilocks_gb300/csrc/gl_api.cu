@@ -23,6 +23,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/goldilocks_gpu.h"
@@ -364,60 +365,133 @@ extern "C" int gl_profile_read(gl_profile_entry *out, int cap) {
 
 // ---------------------------------------------------------------- execution
 
-static const uint32_t kMaxGridY = 65535;
+static const uint64_t kMaxGridYZ = 65535;
 
-// Queue the transform of `count` contiguous transforms at device pointer
-// `data` on `stream`, using `scratch` (>= size*count words) for kind 2.
-static int run_device(gl_plan *pl, uint64_t *data, uint64_t count, bool inv, uint64_t *scratch,
-                      cudaStream_t stream) {
-  if (pl->kind == 0 || count == 0) return GL_OK;
+// Optional load-side transformation (the LDE's zero padding and coset shift).
+struct gl_load_opts {
+  uint32_t in_limit = 0xffffffffu;   // rows >= in_limit read as zero
+  const uint64_t *itw_lo = nullptr;  // g^e, e < 4096
+  const uint64_t *itw_hi = nullptr;  // g^(4096 e)
+};
+
+// Queue the transform of a strided batch on `stream`.  Element j of column c
+// of batch item b is at base[b*bs + j*C + c] (C = 1, bs = n: contiguous
+// transforms; C = cols, B = 1: the columns of a row-major matrix).  `src` and
+// `dst` may be equal.  Two-pass plans use `scratch` (>= n*C*B words).
+static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64_t C,
+                             uint64_t B, uint64_t bs, bool inv, uint64_t *scratch,
+                             cudaStream_t stream, const gl_load_opts *lo = nullptr) {
+  if (B == 0 || C == 0) return GL_OK;
+  const uint64_t n = pl->size;
+  gl_load_opts none;
+  if (!lo) lo = &none;
+  if (pl->kind == 0) {
+    if (src != dst) {
+      for (uint64_t b = 0; b < B; b++) {
+        cudaError_t e = cudaMemcpyAsync(dst + b * bs, src + b * bs, n * C * sizeof(uint64_t),
+                                        cudaMemcpyDeviceToDevice, stream);
+        if (e != cudaSuccess) return cuda_status(e);
+      }
+    }
+    return GL_OK;
+  }
   gl_dev_tables *t = nullptr;
   int st = plan_tables(pl, &t);
   if (st != GL_OK) return st;
   const int d = inv ? 1 : 0;
-  const uint64_t n = pl->size;
+  const bool coset = lo->itw_lo != nullptr;
+  auto base_args = [&]() {
+    gl_pass_args a{};
+    a.in_limit = lo->in_limit;
+    a.tw_lane_div = 1;
+    return a;
+  };
   if (pl->kind == 1) {
     const gl_kernel_entry *k = pl->k[0][d];
-    gl_pass_args a{};
-    a.in = data; a.out = data;
-    a.in_ls = (int64_t)n; a.in_is = 1; a.out_ls = (int64_t)n; a.out_is = 1;
-    a.in_bs = 0; a.out_bs = 0;
-    a.flags = 0;
+    gl_pass_args a = base_args();
     a.tw_m = inv ? t->blk_scaled_inv : t->blk[0][0];
     if (inv) a.flags |= GL_PF_SCALE_ALL;
-    // Lanes are batch items; split very large batches across launches.
-    const uint64_t per_launch = (uint64_t)k->lanes * 0x7fffffffull;
-    for (uint64_t off = 0; off < count; off += per_launch) {
-      uint64_t c = std::min(per_launch, count - off);
-      a.in = data + off * n; a.out = data + off * n;
-      a.lanes = (uint32_t)c;
-      dim3 grid((unsigned)((c + k->lanes - 1) / k->lanes), 1);
-      launch(k, 0, a, grid, c * n, stream);
+    if (coset) {
+      a.flags |= GL_PF_IN_TWIDDLE;
+      a.itw_lo = lo->itw_lo; a.itw_hi = lo->itw_hi; a.itw_jmul = C;
+      a.tw_lane_div = 1;  // J = j*C + c is not used: columns share exponents
     }
-  } else {
-    const uint64_t n1 = pl->n1, n2 = pl->n2;
-    const gl_kernel_entry *kc = pl->k[0][d], *kr = pl->k[1][d];
-    for (uint64_t off = 0; off < count; off += kMaxGridY) {
-      const uint64_t c = std::min<uint64_t>(kMaxGridY, count - off);
-      gl_pass_args a{};  // COL: data -> scratch
-      a.in = data + off * n; a.out = scratch + off * n;
-      a.in_ls = 1; a.in_is = (int64_t)n2; a.out_ls = 1; a.out_is = (int64_t)n2;
-      a.in_bs = (int64_t)n; a.out_bs = (int64_t)n;
-      a.lanes = (uint32_t)n2;
-      a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
-      a.tw_m = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
-      launch(kc, 1, a, dim3((unsigned)(n2 / GL_PASS_LANES), (unsigned)c), c * n, stream);
-      gl_pass_args b{};  // ROW: scratch -> data (transposed store)
-      b.in = scratch + off * n; b.out = data + off * n;
+    if (C == 1) {
+      // Lanes are batch items (stride bs).
+      a.in_ls = a.out_ls = (int64_t)bs; a.in_is = a.out_is = 1;
+      if (coset) { a.itw_jmul = 1; a.tw_lane_div = 0xffffffffu; }
+      const uint64_t per = (uint64_t)k->lanes * 0x7fffffffull;
+      for (uint64_t off = 0; off < B; off += per) {
+        const uint64_t c = std::min(per, B - off);
+        a.in = src + off * bs; a.out = dst + off * bs;
+        a.lanes = (uint32_t)c;
+        launch(k, 0, a, dim3((unsigned)((c + k->lanes - 1) / k->lanes)), c * n, stream);
+      }
+    } else {
+      // Lanes are the C interleaved columns; batch items on grid.y.
+      a.in_ls = a.out_ls = 1; a.in_is = a.out_is = (int64_t)C;
+      a.in_bs = a.out_bs = (int64_t)bs;
+      a.flags |= GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
+      if (coset) { a.itw_jmul = 1; a.tw_lane_div = 0xffffffffu; }
+      a.lanes = (uint32_t)C;
+      for (uint64_t off = 0; off < B; off += kMaxGridYZ) {
+        const uint64_t c = std::min(kMaxGridYZ, B - off);
+        a.in = src + off * bs; a.out = dst + off * bs;
+        launch(k, 0, a, dim3((unsigned)((C + k->lanes - 1) / k->lanes), (unsigned)c),
+               c * n * C, stream);
+      }
+    }
+    return cuda_status(cudaGetLastError());
+  }
+  // Four-step: n = n1*n2, j = n2*j1 + j2, k = k1 + n1*k2.
+  const uint64_t n1 = pl->n1, n2 = pl->n2;
+  const gl_kernel_entry *kc = pl->k[0][d], *kr = pl->k[1][d];
+  for (uint64_t off = 0; off < B; off += kMaxGridYZ) {
+    const uint64_t cb = std::min(kMaxGridYZ, B - off);
+    // COL: lanes are (j2, c) pairs, contiguous; n1-point transforms down them.
+    gl_pass_args a = base_args();
+    a.in = src + off * bs; a.out = scratch + off * n * C;
+    a.in_ls = a.out_ls = 1; a.in_is = a.out_is = (int64_t)(n2 * C);
+    a.in_bs = (int64_t)bs; a.out_bs = (int64_t)(n * C);
+    a.lanes = (uint32_t)(n2 * C);
+    a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
+    a.tw_m = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
+    a.tw_lane_div = (uint32_t)C;
+    if (coset) {
+      a.flags |= GL_PF_IN_TWIDDLE;
+      a.itw_lo = lo->itw_lo; a.itw_hi = lo->itw_hi; a.itw_jmul = n2;
+    }
+    const uint64_t lanes1 = n2 * C;
+    if ((lanes1 + GL_PASS_LANES - 1) / GL_PASS_LANES > 0x7fffffffull) return GL_ERR_INVALID;
+    launch(kc, 1, a, dim3((unsigned)((lanes1 + GL_PASS_LANES - 1) / GL_PASS_LANES), (unsigned)cb),
+           cb * n * C, stream);
+    // ROW: n2-point transforms along j2 for every (k1, c); transposed store.
+    gl_pass_args b = base_args();
+    b.tw_m = t->blk[1][d];
+    b.flags = GL_PF_STORE_LANE_FAST;
+    if (C == 1) {
+      b.in = scratch + off * n; b.out = dst + off * bs;
       b.in_ls = (int64_t)n2; b.in_is = 1; b.out_ls = 1; b.out_is = (int64_t)n1;
-      b.in_bs = (int64_t)n; b.out_bs = (int64_t)n;
+      b.in_bs = (int64_t)n; b.out_bs = (int64_t)bs;
       b.lanes = (uint32_t)n1;
-      b.flags = GL_PF_STORE_LANE_FAST;
-      b.tw_m = t->blk[1][d];
-      launch(kr, 2, b, dim3((unsigned)(n1 / GL_PASS_LANES), (unsigned)c), c * n, stream);
+      launch(kr, 2, b, dim3((unsigned)(n1 / GL_PASS_LANES), (unsigned)cb), cb * n, stream);
+    } else {
+      b.in = scratch + off * n * C; b.out = dst + off * bs;
+      b.in_ls = 1; b.in_is = (int64_t)C; b.out_ls = 1; b.out_is = (int64_t)(n1 * C);
+      b.in_bs = (int64_t)(n2 * C); b.out_bs = (int64_t)C;        // grid.y: k1
+      b.in_bs2 = (int64_t)(n * C); b.out_bs2 = (int64_t)bs;      // grid.z: batch
+      b.flags |= GL_PF_LOAD_LANE_FAST;
+      b.lanes = (uint32_t)C;
+      launch(kr, 2, b, dim3((unsigned)((C + GL_PASS_LANES - 1) / GL_PASS_LANES), (unsigned)n1,
+                            (unsigned)cb), cb * n * C, stream);
     }
   }
   return cuda_status(cudaGetLastError());
+}
+
+static int run_device(gl_plan *pl, uint64_t *data, uint64_t count, bool inv, uint64_t *scratch,
+                      cudaStream_t stream) {
+  return enqueue_transform(pl, data, data, 1, count, pl->size, inv, scratch, stream);
 }
 
 static void init_mempool_once() {
@@ -503,6 +577,143 @@ extern "C" int gl_intt(uint64_t *values, uint64_t len, int mem, void *stream) {
   int st = gl_plan_create(len, &pl);
   if (st != GL_OK) return st;
   return gl_plan_execute(pl, values, len, GL_INVERSE, mem, stream);
+}
+
+// ------------------------------------------------- column batches and LDE
+
+// Device buffer for the duration of one call (stream-ordered pool).
+struct gl_tmp {
+  void *p = nullptr;
+  cudaStream_t s = nullptr;
+  int alloc(size_t bytes, cudaStream_t st) {
+    s = st;
+    if (bytes == 0) return GL_OK;
+    return cuda_status(cudaMallocAsync(&p, bytes, st));
+  }
+  ~gl_tmp() { if (p) cudaFreeAsync(p, s); }
+  uint64_t *u64() { return (uint64_t *)p; }
+};
+
+extern "C" int gl_ntt_columns(uint64_t *data, uint64_t rows, uint64_t cols, int dir, int mem,
+                              void *stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if ((!data && rows * cols) || (dir != GL_FORWARD && dir != GL_INVERSE) ||
+      (mem != GL_MEM_HOST && mem != GL_MEM_DEVICE))
+    return GL_ERR_INVALID;
+  if (rows == 0 || cols == 0) return rows == 0 ? GL_ERR_UNSUPPORTED_SIZE : GL_OK;
+  if (dir == GL_INVERSE && rows == 1) return GL_OK;
+  gl_plan *pl = nullptr;
+  int st = gl_plan_create(rows, &pl);
+  if (st != GL_OK) return st;
+  init_mempool_once();
+  const uint64_t len = rows * cols;
+  const size_t scratch = pl->kind == 2 ? len * sizeof(uint64_t) : 0;
+  if (mem == GL_MEM_DEVICE) {
+    gl_tmp tmp;
+    if ((st = tmp.alloc(scratch, stream)) != GL_OK) return st;
+    return enqueue_transform(pl, data, data, cols, 1, len, dir == GL_INVERSE, tmp.u64(), stream);
+  }
+  int st2 = GL_OK;
+  {
+    gl_tmp dbuf;
+    if ((st = dbuf.alloc(len * sizeof(uint64_t) + scratch, stream)) != GL_OK) return st;
+    cudaError_t e = cudaMemcpyAsync(dbuf.u64(), data, len * 8, cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    st = enqueue_transform(pl, dbuf.u64(), dbuf.u64(), cols, 1, len, dir == GL_INVERSE,
+                           scratch ? dbuf.u64() + len : nullptr, stream);
+    if (st == GL_OK)
+      st = cuda_status(cudaMemcpyAsync(data, dbuf.u64(), len * 8, cudaMemcpyDeviceToHost, stream));
+  }
+  st2 = cuda_status(cudaStreamSynchronize(stream));
+  return st != GL_OK ? st : st2;
+}
+
+// Coset tables g^e (e < 4096) and g^(4096 e) (e < ceil(n/4096)), cached per
+// (device, g, n).
+static std::mutex g_coset_mu;
+static std::map<std::tuple<int, uint64_t, uint64_t>, std::pair<uint64_t *, uint64_t *>> g_coset;
+
+static int coset_tables(uint64_t g, uint64_t n, const uint64_t **lo, const uint64_t **hi) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e);
+  std::lock_guard<std::mutex> lk(g_coset_mu);
+  auto key = std::make_tuple(dev, g, n);
+  auto it = g_coset.find(key);
+  if (it == g_coset.end()) {
+    gl_dev_tables holder;
+    uint64_t *a = nullptr, *b = nullptr;
+    int st = upload(holder, powers(g, GL_TW_SPLIT, 1), &a);
+    if (st == GL_OK)
+      st = upload(holder, powers(gl_pow(g, GL_TW_SPLIT), (n + GL_TW_SPLIT - 1) / GL_TW_SPLIT, 1), &b);
+    if (st != GL_OK) {
+      for (void *p : holder.owned) cudaFree(p);
+      return st;
+    }
+    it = g_coset.emplace(key, std::make_pair(a, b)).first;
+  }
+  *lo = it->second.first;
+  *hi = it->second.second;
+  return GL_OK;
+}
+
+// Device part of the LDE: in (n x cols) -> out (blowup*n x cols), row-major.
+static int lde_device(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t cols,
+                      uint32_t blowup, uint64_t shift, cudaStream_t stream) {
+  const uint64_t m = n * (uint64_t)blowup;
+  gl_plan *pn = nullptr, *pm = nullptr;
+  int st = gl_plan_create(n, &pn);
+  if (st == GL_OK) st = gl_plan_create(m, &pm);
+  if (st != GL_OK) return st;
+  // The forward pass reads only the first n rows of the zero-padded input: in
+  // the four-step view j = n2*j1 + j2 that is j1 < n / n2, so n2 must divide n.
+  if (pm->kind == 2 && n % pm->n2 != 0) return GL_ERR_UNSUPPORTED_SIZE;
+  const uint64_t *clo = nullptr, *chi = nullptr;
+  if ((st = coset_tables(shift % GL_P, n, &clo, &chi)) != GL_OK) return st;
+  // Coefficients (n x cols) plus scratch for the larger of the two transforms.
+  const uint64_t nc = n * cols, mc = m * cols;
+  const uint64_t scratch_words = std::max(pn->kind == 2 ? nc : 0, pm->kind == 2 ? mc : 0);
+  gl_tmp tmp;
+  if ((st = tmp.alloc((nc + scratch_words) * sizeof(uint64_t), stream)) != GL_OK) return st;
+  uint64_t *coef = tmp.u64(), *scr = tmp.u64() + nc;
+  if (n == 1) {
+    cudaError_t e = cudaMemcpyAsync(coef, in, nc * 8, cudaMemcpyDeviceToDevice, stream);
+    if (e != cudaSuccess) return cuda_status(e);
+  } else if ((st = enqueue_transform(pn, in, coef, cols, 1, nc, true, scr, stream)) != GL_OK) {
+    return st;
+  }
+  gl_load_opts lo;
+  lo.in_limit = (uint32_t)(pm->kind == 2 ? n / pm->n2 : n);
+  lo.itw_lo = clo;
+  lo.itw_hi = chi;
+  if (pm->kind == 0) {  // m == 1: the value is the constant coefficient
+    cudaError_t e = cudaMemcpyAsync(out, coef, nc * 8, cudaMemcpyDeviceToDevice, stream);
+    return cuda_status(e);
+  }
+  return enqueue_transform(pm, coef, out, cols, 1, mc, false, scr, stream, &lo);
+}
+
+extern "C" int gl_coset_lde(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t cols,
+                            uint32_t blowup, uint64_t shift, int mem, void *stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (!in || !out || cols == 0 || blowup == 0) return GL_ERR_INVALID;
+  if (mem != GL_MEM_HOST && mem != GL_MEM_DEVICE) return GL_ERR_INVALID;
+  if (!gl_is_divisor(n) || !gl_is_divisor(n * (uint64_t)blowup)) return GL_ERR_UNSUPPORTED_SIZE;
+  init_mempool_once();
+  if (mem == GL_MEM_DEVICE) return lde_device(in, out, n, cols, blowup, shift, stream);
+  const uint64_t nc = n * cols, mc = nc * blowup;
+  int st;
+  {
+    gl_tmp dbuf;
+    if ((st = dbuf.alloc((nc + mc) * sizeof(uint64_t), stream)) != GL_OK) return st;
+    cudaError_t e = cudaMemcpyAsync(dbuf.u64(), in, nc * 8, cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    st = lde_device(dbuf.u64(), dbuf.u64() + nc, n, cols, blowup, shift, stream);
+    if (st == GL_OK)
+      st = cuda_status(cudaMemcpyAsync(out, dbuf.u64() + nc, mc * 8, cudaMemcpyDeviceToHost, stream));
+  }
+  int st2 = cuda_status(cudaStreamSynchronize(stream));
+  return st != GL_OK ? st : st2;
 }
 
 // ------------------------------------------------------------------ inputs

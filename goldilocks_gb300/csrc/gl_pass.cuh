@@ -7,34 +7,49 @@
 //   twiddle:                 Y[kA][jB] *= omega_m^(jB*kA)
 //   round 2: per (lane, kA)  X[kA + MA*kB] = DFT_MB over jB of Y[kA][jB]
 //
-// The same kernel serves the three roles of the four-step schedule by its
-// strides: COL (pass 1: lanes are adjacent columns of an n1 x n2 row-major
-// matrix, transforms run down the columns, and outputs are multiplied by the
-// four-step twiddle omega_n^(col*k)), ROW (pass 2: lanes are adjacent rows;
-// outputs go to the transposed position row + n1*k), and FULL (whole
-// transforms of length m, lanes are batch items).
+// Strides place the lanes and indices anywhere in memory, so one kernel serves
+// every role of the four-step schedule:
+//   COL  pass 1 of a four-step n = n1*n2: lanes are adjacent columns of the
+//        n1 x (n2*C) row-major view, transforms run down the columns, outputs
+//        are multiplied by omega_n^(col*k) with col = lane / C;
+//   ROW  pass 2: lanes are rows (C = 1) or interleaved columns (C > 1);
+//        outputs go to the transposed position k1 + n1*k;
+//   FULL whole transforms of length m; lanes are batch items or columns.
+// Optional on load: zero padding (indices >= in_limit read as zero) and a
+// coset factor g^J, J = j*itw_jmul + lane/C, for the low-degree extension.
 #pragma once
 #include "gl_codelets.cuh"
 
 enum : uint32_t {
-  GL_PF_PASS_TWIDDLE = 1u,  // multiply outputs by omega_n^(lane*k) (COL)
-  GL_PF_SCALE_ALL = 2u,     // tw_m carries a scale: multiply kA = 0 as well
+  GL_PF_PASS_TWIDDLE = 1u,     // outputs *= omega_n^((lane / tw_lane_div) * k)
+  GL_PF_SCALE_ALL = 2u,        // tw_m carries a scale: multiply kA = 0 as well
   GL_PF_LOAD_LANE_FAST = 4u,   // adjacent threads take adjacent lanes on load
   GL_PF_STORE_LANE_FAST = 8u,  // adjacent threads take adjacent lanes on store
+  GL_PF_IN_TWIDDLE = 16u,      // inputs *= g^(j*itw_jmul + lane / tw_lane_div)
 };
 
 struct gl_pass_args {
   const uint64_t *in;
   uint64_t *out;
-  int64_t in_ls, in_is;    // element strides between lanes / between indices
+  int64_t in_ls, in_is;      // element strides between lanes / between indices
   int64_t out_ls, out_is;
-  int64_t in_bs, out_bs;   // element stride between batch items (grid.y)
-  uint32_t lanes;          // lanes per batch item
+  int64_t in_bs, out_bs;     // stride between grid.y batch items
+  int64_t in_bs2, out_bs2;   // stride between grid.z batch items
+  uint32_t lanes;            // lanes per batch item
   uint32_t flags;
-  const uint64_t *tw_m;    // omega_m^e for e < m (direction applied, maybe scaled)
-  const uint64_t *tw_lo;   // omega_n^e, e < 4096 (pass twiddle, maybe scaled)
-  const uint64_t *tw_hi;   // omega_n^(4096 e)
+  uint32_t in_limit;         // indices j >= in_limit load as zero
+  uint32_t tw_lane_div;      // lane -> column index divisor (C)
+  const uint64_t *tw_m;      // omega_m^e for e < m (direction applied, maybe scaled)
+  const uint64_t *tw_lo;     // pass twiddle omega_n^e, e < 4096 (maybe scaled)
+  const uint64_t *tw_hi;     // omega_n^(4096 e)
+  const uint64_t *itw_lo;    // input twiddle g^e, e < 4096
+  const uint64_t *itw_hi;    // g^(4096 e)
+  uint64_t itw_jmul;
 };
+
+__device__ __forceinline__ uint64_t gl_tw2(const uint64_t *lo, const uint64_t *hi, uint64_t e) {
+  return gl_mul(lo[e & 4095], hi[e >> 12]);
+}
 
 template <int MA, int MB>
 struct gl_tile_layout {
@@ -60,8 +75,8 @@ gl_pass_kernel(const gl_pass_args a) {
 
   const int t = threadIdx.x;
   const int64_t lane0 = (int64_t)blockIdx.x * LANES;
-  const uint64_t *in = a.in + (int64_t)blockIdx.y * a.in_bs;
-  uint64_t *out = a.out + (int64_t)blockIdx.y * a.out_bs;
+  const uint64_t *in = a.in + (int64_t)blockIdx.y * a.in_bs + (int64_t)blockIdx.z * a.in_bs2;
+  uint64_t *out = a.out + (int64_t)blockIdx.y * a.out_bs + (int64_t)blockIdx.z * a.out_bs2;
   const bool scale_all = (a.flags & GL_PF_SCALE_ALL) != 0;
 
   // ---- round 1: DFT_MA over jA for one (lane, jB) ----
@@ -73,7 +88,18 @@ gl_pass_kernel(const gl_pass_args a) {
   {
     const uint64_t *src = in + (lane0 + c) * a.in_ls + (int64_t)jB * a.in_is;
 #pragma unroll
-    for (int jA = 0; jA < MA; jA++) x[jA] = live ? src[(int64_t)(MB * jA) * a.in_is] : 0;
+    for (int jA = 0; jA < MA; jA++) {
+      const uint32_t j = (uint32_t)(MB * jA + jB);
+      x[jA] = (live && j < a.in_limit) ? src[(int64_t)(MB * jA) * a.in_is] : 0;
+    }
+    if (a.flags & GL_PF_IN_TWIDDLE) {
+      const uint64_t col = (uint64_t)(lane0 + c) / a.tw_lane_div;
+#pragma unroll
+      for (int jA = 0; jA < MA; jA++) {
+        const uint64_t j = (uint64_t)(MB * jA + jB);
+        if (j < a.in_limit) x[jA] = gl_mul(x[jA], gl_tw2(a.itw_lo, a.itw_hi, j * a.itw_jmul + col));
+      }
+    }
   }
   gl_dft<MA, INV>(x);
   if constexpr (MB > 1) {
@@ -90,8 +116,15 @@ gl_pass_kernel(const gl_pass_args a) {
     // Single round: kA is the output index.
     if (live) {
       uint64_t *dst = out + (lane0 + c) * a.out_ls;
+      if (a.flags & GL_PF_PASS_TWIDDLE) {
+        const uint64_t col = (uint64_t)(lane0 + c) / a.tw_lane_div;
 #pragma unroll
-      for (int kA = 0; kA < MA; kA++) dst[(int64_t)kA * a.out_is] = x[kA];
+        for (int kA = 0; kA < MA; kA++)
+          dst[(int64_t)kA * a.out_is] = gl_mul(x[kA], gl_tw2(a.tw_lo, a.tw_hi, col * kA));
+      } else {
+#pragma unroll
+        for (int kA = 0; kA < MA; kA++) dst[(int64_t)kA * a.out_is] = x[kA];
+      }
     }
     return;
   } else {
@@ -112,12 +145,11 @@ gl_pass_kernel(const gl_pass_args a) {
       if (lane < (int64_t)a.lanes) {
         uint64_t *dst = out + lane * a.out_ls;
         if (a.flags & GL_PF_PASS_TWIDDLE) {
+          const uint64_t col = (uint64_t)lane / a.tw_lane_div;
 #pragma unroll
           for (int kB = 0; kB < MB; kB++) {
             const uint64_t k = (uint64_t)(kA + MA * kB);
-            const uint64_t e = (uint64_t)lane * k;
-            const uint64_t w = gl_mul(a.tw_lo[e & 4095], a.tw_hi[e >> 12]);
-            dst[(int64_t)k * a.out_is] = gl_mul(y[kB], w);
+            dst[(int64_t)k * a.out_is] = gl_mul(y[kB], gl_tw2(a.tw_lo, a.tw_hi, col * k));
           }
         } else {
 #pragma unroll

@@ -101,6 +101,23 @@ int gl_intt(uint64_t *values, uint64_t len, int mem, void *stream);
 /* ntt::clear_cache: forget cached plans (handles already returned stay valid). */
 void gl_clear_cache(void);
 
+/* ---- column batches and the coset LDE (no counterpart in the reference) ---- */
+
+/* Transform every column of the row-major rows x cols matrix `data` in place
+ * (rows must divide p - 1).  Used for batches of polynomials stored
+ * column-interleaved, as a polynomial-commitment matrix is. */
+int gl_ntt_columns(uint64_t *data, uint64_t rows, uint64_t cols, int dir, int mem, void *stream);
+
+/* Reed-Solomon coset low-degree extension of every column of the row-major
+ * n x cols matrix `in`: per column intt(n) (ntt/src/ntt/mod.rs:104-120),
+ * coefficient i multiplied by shift^i, zero-padded to blowup*n and ntt(blowup*n)
+ * (mod.rs:98-102) -- i.e. the evaluations of the column's interpolant on the
+ * coset shift*<omega_{blowup*n}>.  `out` is row-major (blowup*n) x cols and
+ * must not overlap `in`.  The reference has no LDE; this composition of its
+ * intt and ntt defines it. */
+int gl_coset_lde(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t cols, uint32_t blowup,
+                 uint64_t shift, int mem, void *stream);
+
 /* Fill out[0..n) with field elements uniform in [0, p): element i is the
  * first of splitmix64(splitmix64(seed) ^ (offset + i + (k << 48))), k = 0, 1,
  * ..., that is below p.  Host memory; the bench and tests use it for seeded
