@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -116,13 +117,38 @@ static std::string reference_tree(uint64_t size) {
 
 // ----------------------------------------------------------- kernel lookup
 
-const gl_kernel_entry *gl_find_kernel(uint64_t m, bool full, bool inv) {
-  size_t cnt = 0;
-  const gl_kernel_entry *e = full ? (inv ? gl_kernels_full_inv(&cnt) : gl_kernels_full_fwd(&cnt))
-                                  : (inv ? gl_kernels_pass_inv(&cnt) : gl_kernels_pass_fwd(&cnt));
+// GOLDILOCKS_PASS_KERNELS=wide selects the two-round kernels (64 elements
+// per thread) for the four-step passes where one exists; the default is the
+// three-round radix-16 kernels.
+static bool use_wide_kernels() {
+  static const bool wide = [] {
+    const char *v = getenv("GOLDILOCKS_PASS_KERNELS");
+    return v && strcmp(v, "wide") == 0;
+  }();
+  return wide;
+}
+
+static const gl_kernel_entry *find_in(const gl_kernel_entry *e, size_t cnt, uint64_t m) {
   for (size_t i = 0; i < cnt; i++)
     if ((uint64_t)e[i].m == m) return &e[i];
   return nullptr;
+}
+
+const gl_kernel_entry *gl_find_kernel(uint64_t m, bool full, bool inv) {
+  size_t cnt = 0;
+  if (!full && use_wide_kernels()) {
+    const gl_kernel_entry *e = inv ? gl_kernels_wide_inv(&cnt) : gl_kernels_wide_fwd(&cnt);
+    if (const gl_kernel_entry *k = find_in(e, cnt, m)) return k;
+  }
+  const gl_kernel_entry *e = full ? (inv ? gl_kernels_full_inv(&cnt) : gl_kernels_full_fwd(&cnt))
+                                  : (inv ? gl_kernels_pass_inv(&cnt) : gl_kernels_pass_fwd(&cnt));
+  return find_in(e, cnt, m);
+}
+
+static std::string kernel_shape(const gl_kernel_entry *k) {
+  std::string s = std::to_string(k->m) + " (" + std::to_string(k->r1) + "x" + std::to_string(k->r2);
+  if (k->r3) s += "x" + std::to_string(k->r3);
+  return s + ")";
 }
 
 // ------------------------------------------------------------------- plans
@@ -281,9 +307,7 @@ extern "C" uint64_t gl_plan_len(const gl_plan *plan) { return plan ? plan->size 
 extern "C" int gl_plan_describe(const gl_plan *plan, char *buf, size_t cap) {
   if (!plan || !buf) return GL_ERR_INVALID;
   std::string s = plan->tree + " | gpu: ";
-  auto kname = [](const gl_kernel_entry *k) {
-    return std::to_string(k->m) + " (" + std::to_string(k->ma) + "x" + std::to_string(k->mb) + ")";
-  };
+  auto kname = [](const gl_kernel_entry *k) { return kernel_shape(k); };
   if (plan->kind == 0) s += "no-op";
   else if (plan->kind == 1) s += "full " + kname(plan->k[0][0]);
   else s += "col " + kname(plan->k[0][0]) + " + row " + kname(plan->k[1][0]);
@@ -312,8 +336,7 @@ static std::vector<gl_prof_rec> g_prof;
 
 static std::string kernel_label(const gl_kernel_entry *k, int role) {
   static const char *roles[] = {"full", "col", "row"};
-  return std::string(roles[role]) + " " + std::to_string(k->m) + " (" + std::to_string(k->ma) +
-         "x" + std::to_string(k->mb) + ")";
+  return std::string(roles[role]) + " " + kernel_shape(k);
 }
 
 // Launch `k` with optional event bracketing.  role: 0 full, 1 col, 2 row.
@@ -410,6 +433,7 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
     const gl_kernel_entry *k = pl->k[0][d];
     gl_pass_args a = base_args();
     a.tw_m = inv ? t->blk_scaled_inv : t->blk[0][0];
+    a.tw_r2 = t->blk[0][d];
     if (inv) a.flags |= GL_PF_SCALE_ALL;
     if (coset) {
       a.flags |= GL_PF_IN_TWIDDLE;
@@ -455,7 +479,7 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
     a.in_bs = (int64_t)bs; a.out_bs = (int64_t)(n * C);
     a.lanes = (uint32_t)(n2 * C);
     a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
-    a.tw_m = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
+    a.tw_m = a.tw_r2 = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
     a.tw_lane_div = (uint32_t)C;
     if (coset) {
       a.flags |= GL_PF_IN_TWIDDLE;
@@ -467,7 +491,8 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
            cb * n * C, stream);
     // ROW: n2-point transforms along j2 for every (k1, c); transposed store.
     gl_pass_args b = base_args();
-    b.tw_m = t->blk[1][d];
+    b.in_limit = 0xffffffffu;  // zero padding applies to the first pass only
+    b.tw_m = b.tw_r2 = t->blk[1][d];
     b.flags = GL_PF_STORE_LANE_FAST;
     if (C == 1) {
       b.in = scratch + off * n; b.out = dst + off * bs;

@@ -1,6 +1,8 @@
-// Goldilocks field arithmetic, p = 2^64 - 2^32 + 1, for sm_103a device code
-// (the same source also compiles for the host so that the arithmetic can be
-// checked on a CPU).
+// Goldilocks field arithmetic, p = 2^64 - 2^32 + 1, for sm_103a device code.
+// The same source compiles for the host (portable C++ branches) so that the
+// arithmetic and the generated codelets can be checked on a CPU; the device
+// branches are hand-written PTX carry chains on 32-bit halves, because the
+// integer ALU pipe (IADD3/SEL/SHF/ISETP) is the bottleneck of these kernels.
 //
 // Values are canonical u64 in [0, p).  The reference keeps the Montgomery form
 // x*2^64 mod p (ntt/src/field/mod.rs:12); every operation on the transform path
@@ -23,6 +25,30 @@
 #define GL_P 0xffffffff00000001ull
 #define GL_EPS 0x00000000ffffffffull  // 2^64 mod p
 
+#if defined(__CUDA_ARCH__)
+#define GL_DEV_PTX 1
+__device__ __forceinline__ uint64_t gl_pack(uint32_t lo, uint32_t hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "r"(lo), "r"(hi));
+  return r;
+}
+__device__ __forceinline__ void gl_unpack(uint64_t x, uint32_t &lo, uint32_t &hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "l"(x));
+}
+// x >= p  <=>  hi == 0xffffffff and lo != 0; then x - p = lo - 1.
+__device__ __forceinline__ uint64_t gl_canon32(uint32_t lo, uint32_t hi) {
+  uint32_t r0, r1;
+  asm("{\n\t.reg .pred q;\n\t"
+      "setp.eq.u32 q, %3, 0xffffffff;\n\t"
+      "setp.ne.and.u32 q, %2, 0, q;\n\t"
+      "selp.u32 %1, 0, %3, q;\n\t"
+      "sub.u32 %0, %2, 1;\n\t"
+      "selp.u32 %0, %0, %2, q;\n\t}"
+      : "=&r"(r0), "=&r"(r1) : "r"(lo), "r"(hi));
+  return gl_pack(r0, r1);
+}
+#endif
+
 GL_HD uint64_t gl_umulhi(uint64_t a, uint64_t b) {
 #if defined(__CUDA_ARCH__)
   return __umul64hi(a, b);
@@ -31,33 +57,58 @@ GL_HD uint64_t gl_umulhi(uint64_t a, uint64_t b) {
 #endif
 }
 
-// a + b mod p for canonical a, b.  s = a + b; if a + b >= p (carry out of
-// s, or carry out of s + EPS) the result is s + EPS mod 2^64 = a + b - p.
-GL_HD uint64_t gl_add(uint64_t a, uint64_t b) {
-#if defined(__CUDA_ARCH__)
-  uint32_t s0, s1, t0, t1, c;
-  asm("add.cc.u32 %0, %5, %7;\n\t"
-      "addc.cc.u32 %1, %6, %8;\n\t"
-      "addc.u32 %4, 0, 0;\n\t"
-      "add.cc.u32 %2, %0, 0xffffffff;\n\t"
-      "addc.cc.u32 %3, %1, 0;\n\t"
-      "addc.u32 %4, %4, 0;\n\t"
-      : "=&r"(s0), "=&r"(s1), "=&r"(t0), "=&r"(t1), "=&r"(c)
-      : "r"((uint32_t)a), "r"((uint32_t)(a >> 32)), "r"((uint32_t)b), "r"((uint32_t)(b >> 32)));
-  uint32_t r0 = c ? t0 : s0, r1 = c ? t1 : s1;
-  return ((uint64_t)r1 << 32) | r0;
+// Any u64 -> canonical (one conditional subtraction of p).
+GL_HD uint64_t gl_canon(uint64_t x) {
+#ifdef GL_DEV_PTX
+  uint32_t lo, hi;
+  gl_unpack(x, lo, hi);
+  return gl_canon32(lo, hi);
 #else
-  uint64_t s = a + b;
-  uint64_t t = s + GL_EPS;
-  bool wrap = (s < a) | (t < s);
-  return wrap ? t : s;
+  return x >= GL_P ? x - GL_P : x;
 #endif
 }
 
 // a - b mod p for canonical a, b: on borrow add p, i.e. subtract EPS.
 GL_HD uint64_t gl_sub(uint64_t a, uint64_t b) {
+#ifdef GL_DEV_PTX
+  uint32_t a0, a1, b0, b1, r0, r1, m;
+  gl_unpack(a, a0, a1);
+  gl_unpack(b, b0, b1);
+  asm("sub.cc.u32 %0, %3, %5;\n\t"
+      "subc.cc.u32 %1, %4, %6;\n\t"
+      "subc.u32 %2, 0, 0;\n\t"      // m = borrow ? 0xffffffff : 0  (= borrow * EPS)
+      "sub.cc.u32 %0, %0, %2;\n\t"
+      "subc.u32 %1, %1, 0;"
+      : "=&r"(r0), "=&r"(r1), "=&r"(m) : "r"(a0), "r"(a1), "r"(b0), "r"(b1));
+  return gl_pack(r0, r1);
+#else
   uint64_t d = a - b;
   return (a < b) ? d - GL_EPS : d;
+#endif
+}
+
+// a + b mod p for canonical a, b, as a - (p - b) (generic.rs:19-26); p - b is
+// exact in 64 bits (b = 0 gives p, which the borrow path handles).
+GL_HD uint64_t gl_add(uint64_t a, uint64_t b) {
+#ifdef GL_DEV_PTX
+  uint32_t a0, a1, b0, b1, n0, n1, r0, r1, m;
+  gl_unpack(a, a0, a1);
+  gl_unpack(b, b0, b1);
+  asm("sub.cc.u32 %2, 1, %7;\n\t"
+      "subc.u32 %3, 0xffffffff, %8;\n\t"   // n = p - b
+      "sub.cc.u32 %0, %5, %2;\n\t"
+      "subc.cc.u32 %1, %6, %3;\n\t"
+      "subc.u32 %4, 0, 0;\n\t"
+      "sub.cc.u32 %0, %0, %4;\n\t"
+      "subc.u32 %1, %1, 0;"
+      : "=&r"(r0), "=&r"(r1), "=&r"(n0), "=&r"(n1), "=&r"(m)
+      : "r"(a0), "r"(a1), "r"(b0), "r"(b1));
+  return gl_pack(r0, r1);
+#else
+  uint64_t nb = GL_P - b;
+  uint64_t r = a - nb;
+  return (a < nb) ? r - GL_EPS : r;
+#endif
 }
 
 GL_HD uint64_t gl_neg(uint64_t a) { return a ? GL_P - a : 0; }
@@ -74,13 +125,63 @@ GL_HD uint64_t gl_reduce159(uint64_t low, uint64_t mid, uint64_t high) {
   return r;
 }
 
+#ifdef GL_DEV_PTX
+// l + h0*2^64 - h1*2^96 ... as 32-bit words: value = (l1:l0) - h1 + h0*EPS,
+// with h0, h1 < 2^32; canonical result.
+__device__ __forceinline__ uint64_t gl_reduce_words(uint32_t l0, uint32_t l1, uint32_t h0,
+                                                    uint32_t h1) {
+  uint32_t t0, t1, m, u0, u1, c;
+  asm("sub.cc.u32 %0, %6, %9;\n\t"       // t = l - h1
+      "subc.cc.u32 %1, %7, 0;\n\t"
+      "subc.u32 %2, 0, 0;\n\t"
+      "sub.cc.u32 %0, %0, %2;\n\t"       // borrow: + p (t stays >= 0: l - h1 + 2^64 > EPS)
+      "subc.u32 %1, %1, 0;\n\t"
+      "sub.cc.u32 %3, 0, %8;\n\t"        // u = h0 * EPS = h0*2^32 - h0
+      "subc.u32 %4, %8, 0;\n\t"
+      "add.cc.u32 %0, %0, %3;\n\t"       // t += u
+      "addc.cc.u32 %1, %1, %4;\n\t"
+      "addc.u32 %5, 0, 0;\n\t"
+      "sub.u32 %2, 0, %5;\n\t"           // carry: + EPS (cannot wrap again)
+      "add.cc.u32 %0, %0, %2;\n\t"
+      "addc.u32 %1, %1, 0;"
+      : "=&r"(t0), "=&r"(t1), "=&r"(m), "=&r"(u0), "=&r"(u1), "=&r"(c)
+      : "r"(l0), "r"(l1), "r"(h0), "r"(h1));
+  return gl_canon32(t0, t1);
+}
+#endif
+
 // (hi*2^64 + lo) mod p.
 GL_HD uint64_t gl_reduce128(uint64_t lo, uint64_t hi) {
+#ifdef GL_DEV_PTX
+  uint32_t l0, l1, h0, h1;
+  gl_unpack(lo, l0, l1);
+  gl_unpack(hi, h0, h1);
+  return gl_reduce_words(l0, l1, h0, h1);
+#else
   return gl_reduce159(lo, hi & 0xffffffffull, hi >> 32);
+#endif
 }
 
 GL_HD uint64_t gl_mul(uint64_t a, uint64_t b) {
+#ifdef GL_DEV_PTX
+  uint32_t a0, a1, b0, b1, l0, l1, h0, h1;
+  gl_unpack(a, a0, a1);
+  gl_unpack(b, b0, b1);
+  asm("mul.lo.u32 %0, %4, %6;\n\t"
+      "mul.hi.u32 %1, %4, %6;\n\t"
+      "mul.lo.u32 %2, %5, %7;\n\t"
+      "mul.hi.u32 %3, %5, %7;\n\t"
+      "mad.lo.cc.u32 %1, %4, %7, %1;\n\t"
+      "madc.hi.cc.u32 %2, %4, %7, %2;\n\t"
+      "addc.u32 %3, %3, 0;\n\t"
+      "mad.lo.cc.u32 %1, %5, %6, %1;\n\t"
+      "madc.hi.cc.u32 %2, %5, %6, %2;\n\t"
+      "addc.u32 %3, %3, 0;"
+      : "=&r"(l0), "=&r"(l1), "=&r"(h0), "=&r"(h1) : "r"(a0), "r"(a1), "r"(b0), "r"(b1));
+  return gl_reduce_words(l0, l1, h0, h1);
+#else
   return gl_reduce128(a * b, gl_umulhi(a, b));
+#endif
 }
 
 // x * 2^K mod p for a compile-time K in [0, 192).
@@ -91,21 +192,53 @@ GL_HD uint64_t gl_shl(uint64_t x) {
     return x;
   } else if constexpr (K >= 96) {
     return gl_neg(gl_shl<K - 96>(x));     // 2^96 = -1
-  } else if constexpr (K < 64) {
-    // x*2^K < 2^(64+K): low word and a high part < 2^K.
-    uint64_t hi = x >> (64 - K);
-    if constexpr (K <= 32) {
-      return gl_reduce159(x << K, hi, 0);
-    } else {
-      return gl_reduce159(x << K, hi & 0xffffffffull, hi >> 32);
-    }
   } else {
-    // 64 <= K < 96: x*2^K = (a + b*2^32)*2^64 with x*2^(K-64) = a + b*2^32,
-    // = a*2^64 + b*2^96 = a*EPS - b.
-    constexpr int s = K - 64;
-    uint64_t a = (x << s) & 0xffffffffull;
-    uint64_t b = x >> (32 - s);
-    return gl_reduce159(0, a, b);
+#ifdef GL_DEV_PTX
+    // x*2^K as words (w0..w3) of a 160-bit number, then
+    // value = (w1:w0) + w2*2^64 + w3*2^96 with w2, w3 < 2^32.
+    uint32_t x0, x1;
+    gl_unpack(x, x0, x1);
+    uint32_t w0, w1, w2, w3;
+    if constexpr (K < 32) {
+      w0 = x0 << K;
+      w1 = __funnelshift_l(x0, x1, K);
+      w2 = x1 >> (32 - K);
+      w3 = 0;
+    } else if constexpr (K == 32) {
+      w0 = 0; w1 = x0; w2 = x1; w3 = 0;
+    } else if constexpr (K < 64) {
+      w0 = 0;
+      w1 = x0 << (K - 32);
+      w2 = __funnelshift_l(x0, x1, K - 32);
+      w3 = x1 >> (64 - K);
+    } else if constexpr (K == 64) {
+      w0 = 0; w1 = 0; w2 = x0; w3 = x1;
+    } else {
+      w0 = 0;
+      w1 = 0;
+      w2 = x0 << (K - 64);
+      w3 = __funnelshift_l(x0, x1, K - 64);
+    }
+    if constexpr (K > 64) {
+      // 64 < K < 96: x*2^K = w2*2^64 + w3*2^96 + w4*2^128, w4 = x1 >> (96-K);
+      // 2^128 = 2^32 * 2^96 = -2^32, so w4*2^128 = -w4*2^32 (w4 < 2^31).
+      const uint32_t w4 = x1 >> (96 - K);
+      // -w4*2^32 + p as words (1, 0xffffffff - w4), then + w2*2^64 + w3*2^96.
+      return gl_reduce_words(1u, 0xffffffffu - w4, w2, w3);
+    } else {
+      return gl_reduce_words(w0, w1, w2, w3);
+    }
+#else
+    if constexpr (K < 64) {
+      uint64_t hi = x >> (64 - K);
+      return gl_reduce159(x << K, hi & 0xffffffffull, hi >> 32);
+    } else {
+      constexpr int s = K - 64;
+      uint64_t a = (x << s) & 0xffffffffull;
+      uint64_t b = x >> (32 - s);
+      return gl_reduce159(0, a, b);
+    }
+#endif
   }
 }
 

@@ -4,16 +4,18 @@
 #include <stddef.h>
 #include <stdint.h>
 
-#include "gl_pass.cuh"
+#include "gl_pass3.cuh"
 
 typedef void (*gl_launch_fn)(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
 
-// One compiled instance of gl_pass_kernel.
+// One compiled instance of a pass kernel: gl_pass3_kernel (radices r1 x r2 x
+// r3, up to three register rounds) or the two-round gl_pass_kernel (r3 = 0,
+// ma x mb with ma elements per thread).
 struct gl_kernel_entry {
-  int m, ma, mb, lanes;
+  int m, r1, r2, r3, lanes;
   bool inv;
   size_t smem;        // dynamic shared memory bytes
-  int threads;        // LANES * MB
+  int threads;
   gl_launch_fn launch;
 };
 
@@ -24,6 +26,10 @@ const gl_kernel_entry *gl_kernels_full_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_full_inv(size_t *count);
 const gl_kernel_entry *gl_kernels_pass_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_pass_inv(size_t *count);
+// Two-round kernels with up to 64 elements per thread (an alternative the
+// autotuner may choose).
+const gl_kernel_entry *gl_kernels_wide_fwd(size_t *count);
+const gl_kernel_entry *gl_kernels_wide_inv(size_t *count);
 
 // Launch-time check: the kernel entry for (m, full, inv), or nullptr.
 const gl_kernel_entry *gl_find_kernel(uint64_t m, bool full, bool inv);

@@ -1,10 +1,11 @@
-// Four-step column/row pass kernels (LANES = 4), inv.
+// Four-step column/row pass kernels (LANES = 4 lanes per CTA), inv.
 #include "gl_kernels_impl.cuh"
 
 static const gl_kernel_entry k_entries[] = {
-    GL_ENTRY(8, 8, 4, true),    GL_ENTRY(16, 8, 4, true),   GL_ENTRY(16, 16, 4, true),
-    GL_ENTRY(32, 16, 4, true),  GL_ENTRY(32, 32, 4, true),  GL_ENTRY(64, 32, 4, true),
-    GL_ENTRY(64, 64, 4, true),  GL_ENTRY(68, 60, 4, true),
+    GL_ENTRY3(8, 8, 1, 4, 32, true),       GL_ENTRY3(16, 8, 1, 4, 32, true),
+    GL_ENTRY3(16, 16, 1, 4, 64, true),     GL_ENTRY3(8, 8, 8, 4, 256, true),
+    GL_ENTRY3(16, 8, 8, 4, 512, true),     GL_ENTRY3(16, 16, 8, 4, 1024, true),
+    GL_ENTRY3(16, 16, 16, 4, 1024, true),  GL_ENTRY3(16, 15, 17, 4, 1024, true),
 };
 
 const gl_kernel_entry *gl_kernels_pass_inv(size_t *count) {

@@ -1,6 +1,5 @@
-// Instantiates one set of gl_pass_kernel variants.  Included by the
-// gl_kern_*.cu translation units with GL_KSET (0 = full, 1 = pass) and
-// GL_KINV (false/true) defined, so that the sets compile in parallel.
+// Instantiates one set of pass-kernel variants.  Included by the gl_kern_*.cu
+// translation units so that the sets compile in parallel.
 #pragma once
 #include "gl_internal.h"
 
@@ -13,5 +12,17 @@ static void gl_launch_pass(const gl_pass_args &args, dim3 grid, cudaStream_t str
   kern<<<grid, LANES * MB, smem, stream>>>(args);
 }
 
+template <int R1, int R2, int R3, int LANES, int NT, bool INV>
+static void gl_launch_pass3(const gl_pass_args &args, dim3 grid, cudaStream_t stream) {
+  constexpr size_t smem = gl_p3_smem_bytes<R1, R2, R3, LANES>();
+  auto kern = gl_pass3_kernel<R1, R2, R3, LANES, NT, INV>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  kern<<<grid, NT, smem, stream>>>(args);
+}
+
 #define GL_ENTRY(MA, MB, LANES, INV) \
-  {MA * MB, MA, MB, LANES, INV, gl_pass_smem_bytes<MA, MB>(LANES), LANES * MB, gl_launch_pass<MA, MB, LANES, INV>}
+  {MA * MB, MA, MB, 0, LANES, INV, gl_pass_smem_bytes<MA, MB>(LANES), LANES * MB, gl_launch_pass<MA, MB, LANES, INV>}
+
+#define GL_ENTRY3(R1, R2, R3, LANES, NT, INV)                                                 \
+  {R1 * R2 * R3, R1, R2, R3, LANES, INV, gl_p3_smem_bytes<R1, R2, R3, LANES>(), NT,          \
+   gl_launch_pass3<R1, R2, R3, LANES, NT, INV>}

@@ -40,6 +40,7 @@ struct gl_pass_args {
   uint32_t in_limit;         // indices j >= in_limit load as zero
   uint32_t tw_lane_div;      // lane -> column index divisor (C)
   const uint64_t *tw_m;      // omega_m^e for e < m (direction applied, maybe scaled)
+  const uint64_t *tw_r2;     // the same table never scaled (second twiddle stage)
   const uint64_t *tw_lo;     // pass twiddle omega_n^e, e < 4096 (maybe scaled)
   const uint64_t *tw_hi;     // omega_n^(4096 e)
   const uint64_t *itw_lo;    // input twiddle g^e, e < 4096

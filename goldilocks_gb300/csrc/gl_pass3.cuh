@@ -1,0 +1,175 @@
+// Block-DFT pass kernel with up to three register rounds.
+//
+// Every CTA transforms LANES independent m-point sequences ("lanes"),
+// m = R1*R2*R3, held in one shared-memory tile.  Positions are mixed-radix
+// digits p = d1*(R2*R3) + d2*R3 + d3; decimation in frequency:
+//
+//   round 1: DFT_R1 over d1 for each (d2, d3) = jB; then * omega_m^(jB*k1)
+//   round 2: DFT_R2 over d2 for each (k1, d3);     then * omega_(R2 R3)^(d3*k2)
+//   round 3: DFT_R3 over d3 for each (k1, k2)
+//   output frequency k = k1 + R1*k2 + R1*R2*k3.
+//
+// Each thread holds one radix-R group in registers (R <= 17), so the code per
+// round is one straight-line codelet and the kernel runs 1024 threads per
+// CTA.  Round 1 reads global memory directly and the last round writes it;
+// rounds exchange through shared memory (XOR-swizzled against bank
+// conflicts).  Strides give the COL / ROW / FULL roles of gl_pass.cuh; the
+// same flags apply (pass twiddle, zero padding, coset factor, scale).
+#pragma once
+#include "gl_pass.cuh"
+
+template <int R1, int R2, int R3>
+struct gl_p3_layout {
+  static constexpr int M = R1 * R2 * R3;
+  static constexpr int NR = R2 == 1 ? 1 : (R3 == 1 ? 2 : 3);
+  static constexpr int RL = NR == 3 ? R3 : (NR == 2 ? R2 : R1);  // last radix
+  static constexpr bool POW2 = (RL & (RL - 1)) == 0 && (M & (M - 1)) == 0;
+  static constexpr int SH = RL == 16 ? 4 : RL == 8 ? 3 : RL == 4 ? 2 : RL == 2 ? 1 : 0;
+  static constexpr int MSK = POW2 ? (RL < 16 ? RL - 1 : 15) : 0;
+  // Lane stride: a multiple of 16 words plus 4.
+  static constexpr int LS = ((M + 15) / 16) * 16 + 4;
+  static __device__ __forceinline__ int word(int c, int p) {
+    return c * LS + (POW2 ? (p ^ ((p >> SH) & MSK)) : p);
+  }
+};
+
+template <int R1, int R2, int R3, int LANES>
+constexpr size_t gl_p3_smem_bytes() {
+  return gl_p3_layout<R1, R2, R3>::NR == 1 ? 0
+                                            : (size_t)LANES * gl_p3_layout<R1, R2, R3>::LS * 8;
+}
+
+template <int R1, int R2, int R3, int LANES, int NT, bool INV>
+__global__ void __launch_bounds__(NT) gl_pass3_kernel(const gl_pass_args a) {
+  using L = gl_p3_layout<R1, R2, R3>;
+  constexpr int M = L::M;
+  constexpr int S1 = R2 * R3;
+  extern __shared__ uint64_t sm[];
+
+  const int64_t lane0 = (int64_t)blockIdx.x * LANES;
+  const uint64_t *in = a.in + (int64_t)blockIdx.y * a.in_bs + (int64_t)blockIdx.z * a.in_bs2;
+  uint64_t *out = a.out + (int64_t)blockIdx.y * a.out_bs + (int64_t)blockIdx.z * a.out_bs2;
+  const bool scale_all = (a.flags & GL_PF_SCALE_ALL) != 0;
+  const bool load_lane_fast = (a.flags & GL_PF_LOAD_LANE_FAST) != 0;
+  const bool store_lane_fast = (a.flags & GL_PF_STORE_LANE_FAST) != 0;
+
+  // ------------------------------------------------------------- round 1
+  {
+    constexpr int G = M / R1;  // groups per lane: jB = (d2, d3)
+    for (int idx = threadIdx.x; idx < LANES * G; idx += NT) {
+      int c, g;
+      if (load_lane_fast) { c = idx % LANES; g = idx / LANES; }
+      else { g = idx % G; c = idx / G; }
+      const int64_t lane = lane0 + c;
+      const bool live = lane < (int64_t)a.lanes;
+      uint64_t x[R1];
+      const uint64_t *src = in + lane * a.in_ls + (int64_t)g * a.in_is;
+#pragma unroll
+      for (int t = 0; t < R1; t++) {
+        const uint32_t j = (uint32_t)(g + S1 * t);
+        x[t] = (live && j < a.in_limit) ? src[(int64_t)(S1 * t) * a.in_is] : 0;
+      }
+      if (a.flags & GL_PF_IN_TWIDDLE) {
+        const uint64_t col = (uint64_t)lane / a.tw_lane_div;
+#pragma unroll
+        for (int t = 0; t < R1; t++) {
+          const uint64_t j = (uint64_t)(g + S1 * t);
+          if (j < a.in_limit) x[t] = gl_mul(x[t], gl_tw2(a.itw_lo, a.itw_hi, j * a.itw_jmul + col));
+        }
+      }
+      gl_dft<R1, INV>(x);
+      if constexpr (L::NR == 1) {
+        // Single round: t is the output index.
+        if (scale_all) {
+          const uint64_t s = a.tw_m[0];
+#pragma unroll
+          for (int t = 0; t < R1; t++) x[t] = gl_mul(x[t], s);
+        }
+        if (live) {
+          uint64_t *dst = out + lane * a.out_ls;
+          if (a.flags & GL_PF_PASS_TWIDDLE) {
+            const uint64_t col = (uint64_t)lane / a.tw_lane_div;
+#pragma unroll
+            for (int t = 0; t < R1; t++)
+              dst[(int64_t)t * a.out_is] = gl_mul(x[t], gl_tw2(a.tw_lo, a.tw_hi, col * t));
+          } else {
+#pragma unroll
+            for (int t = 0; t < R1; t++) dst[(int64_t)t * a.out_is] = x[t];
+          }
+        }
+      } else {
+#pragma unroll
+        for (int t = 0; t < R1; t++) {
+          uint64_t v = x[t];
+          if (t > 0 || scale_all) v = gl_mul(v, __ldg(a.tw_m + g * t));
+          sm[L::word(c, g + S1 * t)] = v;
+        }
+      }
+    }
+  }
+  if constexpr (L::NR == 1) return;
+  __syncthreads();
+
+  // ------------------------------------------------------------- round 2
+  if constexpr (L::NR == 3) {
+    constexpr int G = R1 * R3;  // groups (k1, d3)
+    for (int idx = threadIdx.x; idx < LANES * G; idx += NT) {
+      const int c = idx % LANES, g = idx / LANES;
+      const int k1 = g / R3, d3 = g % R3;
+      const int base = k1 * S1 + d3;
+      uint64_t x[R2];
+#pragma unroll
+      for (int t = 0; t < R2; t++) x[t] = sm[L::word(c, base + R3 * t)];
+      gl_dft<R2, INV>(x);
+#pragma unroll
+      for (int t = 0; t < R2; t++) {
+        uint64_t v = x[t];
+        if (t > 0) v = gl_mul(v, __ldg(a.tw_r2 + R1 * d3 * t));
+        sm[L::word(c, base + R3 * t)] = v;
+      }
+    }
+    __syncthreads();
+  }
+
+  // ------------------------------------------------------- last round
+  {
+    constexpr int RL = L::NR == 3 ? R3 : R2;
+    constexpr int SL = L::NR == 3 ? R1 * R2 : R1;  // output stride of the last digit
+    constexpr int G = M / RL;                      // groups: (k1, k2) or k1
+    for (int idx = threadIdx.x; idx < LANES * G; idx += NT) {
+      int c, g;
+      if (store_lane_fast) { c = idx % LANES; g = idx / LANES; }
+      else { g = idx % G; c = idx / G; }
+      // group g enumerates (k1, k2) with k2 fastest for 3 rounds (positions
+      // k1*S1 + k2*R3 + t), or k1 for 2 rounds (positions k1*R2 + t).
+      int base, kbase;
+      if constexpr (L::NR == 3) {
+        const int k1 = g / R2, k2 = g % R2;
+        base = k1 * S1 + k2 * R3;
+        kbase = k1 + R1 * k2;
+      } else {
+        base = g * R2;
+        kbase = g;
+      }
+      uint64_t x[RL];
+#pragma unroll
+      for (int t = 0; t < RL; t++) x[t] = sm[L::word(c, base + t)];
+      gl_dft<RL, INV>(x);
+      const int64_t lane = lane0 + c;
+      if (lane < (int64_t)a.lanes) {
+        uint64_t *dst = out + lane * a.out_ls;
+        if (a.flags & GL_PF_PASS_TWIDDLE) {
+          const uint64_t col = (uint64_t)lane / a.tw_lane_div;
+#pragma unroll
+          for (int t = 0; t < RL; t++) {
+            const uint64_t k = (uint64_t)(kbase + SL * t);
+            dst[(int64_t)k * a.out_is] = gl_mul(x[t], gl_tw2(a.tw_lo, a.tw_hi, col * k));
+          }
+        } else {
+#pragma unroll
+          for (int t = 0; t < RL; t++) dst[(int64_t)(kbase + SL * t) * a.out_is] = x[t];
+        }
+      }
+    }
+  }
+}

@@ -1,0 +1,80 @@
+// Host emulation of the pass kernels for CPU tests: the kernel source is
+// compiled as plain C++ (the portable field-arithmetic branches), each CUDA
+// thread of one CTA is a std::thread, and __syncthreads() is a barrier.  The
+// test-suite drives it through ctypes and compares with the oracle.
+#include <stdint.h>
+#include <string.h>
+
+#include <barrier>
+#include <functional>
+#include <thread>
+#include <vector>
+
+struct dim3 {
+  unsigned x = 1, y = 1, z = 1;
+};
+static thread_local dim3 threadIdx;
+static dim3 blockIdx;
+static std::barrier<> *g_bar = nullptr;
+
+#define __global__
+#define __device__
+#define __host__
+#define __forceinline__ inline
+#define __launch_bounds__(...)
+#define __shared__
+#define __syncthreads() g_bar->arrive_and_wait()
+#define __ldg(p) (*(p))
+
+uint64_t sm[1 << 16];  // the CTA's dynamic shared memory
+
+#include "gl_pass3.cuh"
+
+template <int R1, int R2, int R3, int LANES, int NT, bool INV>
+static void run_grid(const gl_pass_args &a, unsigned gx, unsigned gy, unsigned gz) {
+  for (unsigned z = 0; z < gz; z++)
+    for (unsigned y = 0; y < gy; y++)
+      for (unsigned x = 0; x < gx; x++) {
+        blockIdx.x = x; blockIdx.y = y; blockIdx.z = z;
+        memset(sm, 0xA5, sizeof(sm));
+        std::barrier<> bar(NT);
+        g_bar = &bar;
+        std::vector<std::thread> th;
+        for (int t = 0; t < NT; t++)
+          th.emplace_back([&a, t] {
+            threadIdx.x = t;
+            gl_pass3_kernel<R1, R2, R3, LANES, NT, INV>(a);
+          });
+        for (auto &t : th) t.join();
+      }
+}
+
+extern "C" {
+// Emulated launch of one compiled shape; returns -1 for an unknown shape.
+int emu_pass3(int r1, int r2, int r3, int inv, const uint64_t *in, uint64_t *out, int64_t in_ls,
+              int64_t in_is, int64_t out_ls, int64_t out_is, uint32_t lanes, uint32_t flags,
+              const uint64_t *tw_m, const uint64_t *tw_r2, const uint64_t *tw_lo,
+              const uint64_t *tw_hi,
+              uint32_t tw_lane_div, uint32_t in_limit, const uint64_t *itw_lo,
+              const uint64_t *itw_hi, uint64_t itw_jmul) {
+  gl_pass_args a{};
+  a.in = in; a.out = out;
+  a.in_ls = in_ls; a.in_is = in_is; a.out_ls = out_ls; a.out_is = out_is;
+  a.lanes = lanes; a.flags = flags; a.tw_m = tw_m; a.tw_r2 = tw_r2; a.tw_lo = tw_lo; a.tw_hi = tw_hi;
+  a.tw_lane_div = tw_lane_div; a.in_limit = in_limit;
+  a.itw_lo = itw_lo; a.itw_hi = itw_hi; a.itw_jmul = itw_jmul;
+  const unsigned gx = (lanes + 3) / 4;
+#define SHAPE(R1, R2, R3, NT)                                                        \
+  if (r1 == R1 && r2 == R2 && r3 == R3) {                                              \
+    if (inv) run_grid<R1, R2, R3, 4, NT, true>(a, gx, 1, 1);                           \
+    else run_grid<R1, R2, R3, 4, NT, false>(a, gx, 1, 1);                              \
+    return 0;                                                                          \
+  }
+  SHAPE(8, 8, 1, 32)
+  SHAPE(16, 16, 1, 64)
+  SHAPE(8, 8, 8, 256)
+  SHAPE(16, 8, 8, 512)
+  SHAPE(16, 16, 8, 1024)
+  return -1;
+}
+}

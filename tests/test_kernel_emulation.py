@@ -1,0 +1,108 @@
+"""CPU: the pass-kernel source emulated on the host (tests/kernel_emu.cpp: one
+std::thread per CUDA thread, a barrier for __syncthreads) in each role the
+library launches it in, against the oracle.  Catches indexing, twiddle and
+scaling mistakes without a GPU; the device-only PTX arithmetic is covered by
+the GPU tests."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import P, ROOT, rand_field
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+F_PASS_TW, F_SCALE, F_LOAD_LF, F_STORE_LF, F_IN_TW = 1, 2, 4, 8, 16
+NOLIM = 0xFFFFFFFF
+
+
+@pytest.fixture(scope="module")
+def emu(tmp_path_factory):
+    so = tmp_path_factory.mktemp("emu") / "emu.so"
+    subprocess.run(["g++", "-std=c++20", "-O1", "-fPIC", "-shared", "-pthread",
+                    "-I" + os.path.join(ROOT, "goldilocks_gb300", "csrc"),
+                    os.path.join(HERE, "kernel_emu.cpp"), "-o", str(so)], check=True)
+    lib = ctypes.CDLL(str(so))
+    vp, i64, u32, u64 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint64
+    lib.emu_pass3.argtypes = [ctypes.c_int] * 4 + [vp, vp, i64, i64, i64, i64, u32, u32,
+                                                   vp, vp, vp, vp, u32, u32, vp, vp, u64]
+    return lib
+
+
+def root(n, inv=False):
+    w = pow(2717, (P - 1) // n, P)
+    return pow(w, P - 2, P) if inv else w
+
+
+def table(w, count, scale=1):
+    out, x = [], scale
+    for _ in range(count):
+        out.append(x)
+        x = x * w % P
+    return np.array(out, dtype=np.uint64)
+
+
+def call(emu, shape, inv, x, out, in_ls, in_is, out_ls, out_is, lanes, flags, tw_m, tw_r2,
+         tw_lo=None, tw_hi=None, lane_div=1, in_limit=NOLIM, itw_lo=None, itw_hi=None, jmul=0):
+    ptr = lambda a: None if a is None else a.ctypes.data
+    rc = emu.emu_pass3(*shape, int(inv), ptr(x), ptr(out), in_ls, in_is, out_ls, out_is, lanes, flags,
+                       ptr(tw_m), ptr(tw_r2), ptr(tw_lo), ptr(tw_hi), lane_div, in_limit,
+                       ptr(itw_lo), ptr(itw_hi), jmul)
+    assert rc == 0
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 1), (16, 16, 1), (8, 8, 8), (16, 8, 8)])
+@pytest.mark.parametrize("inv", [False, True])
+def test_whole_transforms_on_columns(emu, oracle, shape, inv):
+    m = shape[0] * shape[1] * shape[2]
+    cols = 5
+    x = rand_field(m * cols, seed=m + inv)
+    out = np.zeros_like(x)
+    tw = table(root(m, inv), m)
+    tw_m = table(root(m, inv), m, pow(m, P - 2, P)) if inv else tw
+    call(emu, shape, inv, x, out, 1, cols, 1, cols, cols,
+         F_LOAD_LF | F_STORE_LF | (F_SCALE if inv else 0), tw_m, tw)
+    want = np.stack([(oracle.intt if inv else oracle.ntt)(x.reshape(m, cols)[:, c].copy())
+                     for c in range(cols)], axis=1)
+    assert np.array_equal(out.reshape(m, cols), want)
+
+
+def four_step(emu, n1, n2, shape1, shape2, x, inv=False, C=1, in_limit=NOLIM, coset=None):
+    """COL(n1) then ROW(n2), exactly as the library schedules them."""
+    n = n1 * n2
+    scratch = np.zeros(n * C, dtype=np.uint64)
+    out = np.zeros(n * C, dtype=np.uint64)
+    w = root(n, inv)
+    scale = pow(n, P - 2, P) if inv else 1
+    lo, hi = table(w, 4096, scale), table(pow(w, 4096, P), (n + 4095) // 4096)
+    t1, t2 = table(root(n1, inv), n1), table(root(n2, inv), n2)
+    kw = {}
+    flags = F_PASS_TW | F_LOAD_LF | F_STORE_LF
+    if coset is not None:
+        g = coset
+        kw = dict(in_limit=in_limit, itw_lo=table(g, 4096), itw_hi=table(pow(g, 4096, P), 64), jmul=n2)
+        flags |= F_IN_TW
+    call(emu, shape1, inv, x, scratch, 1, n2 * C, 1, n2 * C, n2 * C, flags, t1, t1, lo, hi,
+         lane_div=C, **kw)
+    assert C == 1
+    call(emu, shape2, inv, scratch, out, n2, 1, 1, n1, n1, F_STORE_LF, t2, t2)
+    return out
+
+
+@pytest.mark.parametrize("inv", [False, True])
+def test_four_step(emu, oracle, inv):
+    n1, n2 = 64, 512
+    x = rand_field(n1 * n2, seed=7 + inv)
+    got = four_step(emu, n1, n2, (8, 8, 1), (8, 8, 8), x, inv)
+    assert np.array_equal(got, (oracle.intt if inv else oracle.ntt)(x))
+
+
+def test_four_step_zero_padded_coset(emu, oracle):
+    """The LDE's forward pass: only the first rows are read, each scaled by g^j."""
+    n1, n2, rows, g = 64, 256, 2048, 7
+    coeffs = rand_field(rows, seed=11)
+    got = four_step(emu, n1, n2, (8, 8, 1), (16, 16, 1), coeffs, in_limit=rows // n2, coset=g)
+    full = np.zeros(n1 * n2, dtype=np.uint64)
+    full[:rows] = [int(c) * pow(g, j, P) % P for j, c in enumerate(coeffs)]
+    assert np.array_equal(got, oracle.ntt(full))
