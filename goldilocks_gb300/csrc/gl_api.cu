@@ -159,6 +159,7 @@ struct gl_dev_tables {
   uint64_t *blk_scaled_inv = nullptr;                               // FULL inverse: omega^-e / n
   uint64_t *tw_lo[2] = {nullptr, nullptr};                          // pass twiddle, [dir]
   uint64_t *tw_hi[2] = {nullptr, nullptr};
+  uint64_t *tw_full[2] = {nullptr, nullptr};  // omega_n^(col*k) at [k*n2 + col], [dir]
   std::vector<void *> owned;
 };
 
@@ -236,6 +237,33 @@ static std::vector<uint64_t> powers(uint64_t w, uint64_t count, uint64_t scale) 
   return v;
 }
 
+// out[k*n2 + col] = omega_n^(col*k) for k < n1, col < n2, from the two-level table.
+__global__ void gl_fill_pass_twiddles(uint64_t *out, const uint64_t *lo, const uint64_t *hi,
+                                      uint64_t n1, uint64_t n2) {
+  const uint64_t total = n1 * n2;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = i / n2, col = i % n2;
+    const uint64_t e = col * k;  // < n1*n2
+    out[i] = gl_mul(lo[e & 4095], hi[e >> 12]);
+  }
+}
+
+// Full pass-twiddle tables (8 bytes per element and direction; one load and
+// one multiplication per element instead of two loads and two) are built for
+// plans up to this size when GOLDILOCKS_PASS_TWIDDLE=full.  Measured on GB300
+// at 2^24 the two-level table is faster (the column pass is bound by the
+// integer pipe, and the table load sits on its critical path), so it is the
+// default.
+static const uint64_t kFullTwiddleMax = 1ull << 26;
+static bool full_twiddles_enabled() {
+  static const bool on = [] {
+    const char *v = getenv("GOLDILOCKS_PASS_TWIDDLE");
+    return v && strcmp(v, "full") == 0;
+  }();
+  return on;
+}
+
 // Twiddle tables for the current device, built on first use.
 static int plan_tables(gl_plan *pl, gl_dev_tables **out) {
   int dev = 0;
@@ -260,6 +288,17 @@ static int plan_tables(gl_plan *pl, gl_dev_tables **out) {
       const uint64_t scale = d ? gl_inv(n % GL_P) : 1;
       if (st == GL_OK) st = upload(t, powers(w, GL_TW_SPLIT, scale), &t.tw_lo[d]);
       if (st == GL_OK) st = upload(t, powers(gl_pow(w, GL_TW_SPLIT), hi_count, 1), &t.tw_hi[d]);
+      if (st == GL_OK && n <= kFullTwiddleMax && full_twiddles_enabled()) {
+        void *p = nullptr;
+        cudaError_t e = cudaMalloc(&p, n * sizeof(uint64_t));
+        if (e != cudaSuccess) { st = cuda_status(e); break; }
+        t.owned.push_back(p);
+        t.tw_full[d] = (uint64_t *)p;
+        const unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 152 * 32);
+        gl_fill_pass_twiddles<<<blocks, 256>>>(t.tw_full[d], t.tw_lo[d], t.tw_hi[d], pl->n1, pl->n2);
+        e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) st = cuda_status(e);
+      }
     }
   }
   if (st != GL_OK) {
@@ -481,6 +520,11 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
     a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
     a.tw_m = a.tw_r2 = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
     a.tw_lane_div = (uint32_t)C;
+    if (t->tw_full[d]) {
+      a.flags |= GL_PF_TW_TABLE;
+      a.tw_full = t->tw_full[d];
+      a.tw_ld = (int64_t)n2;
+    }
     if (coset) {
       a.flags |= GL_PF_IN_TWIDDLE;
       a.itw_lo = lo->itw_lo; a.itw_hi = lo->itw_hi; a.itw_jmul = n2;

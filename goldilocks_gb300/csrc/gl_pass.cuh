@@ -26,6 +26,7 @@ enum : uint32_t {
   GL_PF_LOAD_LANE_FAST = 4u,   // adjacent threads take adjacent lanes on load
   GL_PF_STORE_LANE_FAST = 8u,  // adjacent threads take adjacent lanes on store
   GL_PF_IN_TWIDDLE = 16u,      // inputs *= g^(j*itw_jmul + lane / tw_lane_div)
+  GL_PF_TW_TABLE = 32u,        // pass twiddle from tw_full[k*tw_ld + lane / tw_lane_div]
 };
 
 struct gl_pass_args {
@@ -46,7 +47,16 @@ struct gl_pass_args {
   const uint64_t *itw_lo;    // input twiddle g^e, e < 4096
   const uint64_t *itw_hi;    // g^(4096 e)
   uint64_t itw_jmul;
+  const uint64_t *tw_full;   // full pass-twiddle table omega_n^(col*k) at [k*tw_ld + col]
+  int64_t tw_ld;
 };
+
+// Pass twiddle omega_n^(col*k): from the full table when present, else from
+// the two-level table (two loads, one extra multiplication).
+__device__ __forceinline__ uint64_t gl_pass_tw(const gl_pass_args &a, uint64_t col, uint64_t k) {
+  if (a.flags & GL_PF_TW_TABLE) return __ldg(a.tw_full + (int64_t)k * a.tw_ld + (int64_t)col);
+  return gl_mul(a.tw_lo[(col * k) & 4095], a.tw_hi[(col * k) >> 12]);
+}
 
 __device__ __forceinline__ uint64_t gl_tw2(const uint64_t *lo, const uint64_t *hi, uint64_t e) {
   return gl_mul(lo[e & 4095], hi[e >> 12]);

@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(NT) gl_pass3_kernel(const gl_pass_args a) {
             const uint64_t col = (uint64_t)lane / a.tw_lane_div;
 #pragma unroll
             for (int t = 0; t < R1; t++)
-              dst[(int64_t)t * a.out_is] = gl_mul(x[t], gl_tw2(a.tw_lo, a.tw_hi, col * t));
+              dst[(int64_t)t * a.out_is] = gl_mul(x[t], gl_pass_tw(a, col, t));
           } else {
 #pragma unroll
             for (int t = 0; t < R1; t++) dst[(int64_t)t * a.out_is] = x[t];
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(NT) gl_pass3_kernel(const gl_pass_args a) {
 #pragma unroll
           for (int t = 0; t < RL; t++) {
             const uint64_t k = (uint64_t)(kbase + SL * t);
-            dst[(int64_t)k * a.out_is] = gl_mul(x[t], gl_tw2(a.tw_lo, a.tw_hi, col * k));
+            dst[(int64_t)k * a.out_is] = gl_mul(x[t], gl_pass_tw(a, col, k));
           }
         } else {
 #pragma unroll
