@@ -35,9 +35,19 @@ SIGNATURES = [
     ("gl_fill_uniform", None, [_vp, _u64, _u64, _u64]),
     ("gl_ntt_columns", _int, [_vp, _u64, _u64, _int, _int, _vp]),
     ("gl_coset_lde", _int, [_vp, _vp, _u64, _u64, _u32, _u64, _int, _vp]),
+    ("gl_batch_execute", _int, [_vp, _u64, _int, _vp]),
+    ("gl_batch_autotune", _int, [_vp, _u64, _int, _vp, _vp]),
     ("gl_profile_enable", _int, [_int]),
     ("gl_profile_read", _int, [_vp, _int]),
 ]
+
+
+class Poly(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("len", ctypes.c_uint64), ("dir", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+GL_BATCH_AUTO, GL_BATCH_PERSISTENT, GL_BATCH_BUCKETS, GL_BATCH_PER_CALL = 0, 1, 2, 3
 
 
 class ProfileEntry(ctypes.Structure):

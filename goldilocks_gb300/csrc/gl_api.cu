@@ -48,7 +48,7 @@ extern "C" const char *gl_status_string(int status) {
   }
 }
 
-static int cuda_status(cudaError_t e) {
+int gl_cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return GL_OK;
   if (e == cudaErrorMemoryAllocation) return GL_ERR_OOM;
   return GL_ERR_CUDA;
@@ -153,26 +153,6 @@ static std::string kernel_shape(const gl_kernel_entry *k) {
 
 // ------------------------------------------------------------------- plans
 
-// Device-resident twiddle tables of one plan on one device.
-struct gl_dev_tables {
-  uint64_t *blk[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [stage][dir] omega_m^e
-  uint64_t *blk_scaled_inv = nullptr;                               // FULL inverse: omega^-e / n
-  uint64_t *tw_lo[2] = {nullptr, nullptr};                          // pass twiddle, [dir]
-  uint64_t *tw_hi[2] = {nullptr, nullptr};
-  uint64_t *tw_full[2] = {nullptr, nullptr};  // omega_n^(col*k) at [k*n2 + col], [dir]
-  std::vector<void *> owned;
-};
-
-struct gl_plan {
-  uint64_t size = 0;
-  int kind = 0;                 // 0: no-op (size <= 1), 1: FULL, 2: COL+ROW
-  uint64_t n1 = 0, n2 = 0;      // kind 2: COL over n1, ROW over n2
-  const gl_kernel_entry *k[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [stage][dir]
-  std::string tree;
-  std::mutex mu;
-  std::map<int, gl_dev_tables> dev;  // per device id
-};
-
 static std::mutex g_cache_mu;
 static std::map<uint64_t, gl_plan *> g_cache;
 
@@ -222,9 +202,9 @@ static void choose_schedule(gl_plan *pl) {
 static int upload(gl_dev_tables &t, const std::vector<uint64_t> &h, uint64_t **dst) {
   void *p = nullptr;
   cudaError_t e = cudaMalloc(&p, h.size() * sizeof(uint64_t));
-  if (e != cudaSuccess) return cuda_status(e);
+  if (e != cudaSuccess) return gl_cuda_status(e);
   e = cudaMemcpy(p, h.data(), h.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) { cudaFree(p); return cuda_status(e); }
+  if (e != cudaSuccess) { cudaFree(p); return gl_cuda_status(e); }
   t.owned.push_back(p);
   *dst = (uint64_t *)p;
   return GL_OK;
@@ -265,10 +245,10 @@ static bool full_twiddles_enabled() {
 }
 
 // Twiddle tables for the current device, built on first use.
-static int plan_tables(gl_plan *pl, gl_dev_tables **out) {
+int gl_plan_tables(gl_plan *pl, gl_dev_tables **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_status(e);
+  if (e != cudaSuccess) return gl_cuda_status(e);
   std::lock_guard<std::mutex> lk(pl->mu);
   auto it = pl->dev.find(dev);
   if (it != pl->dev.end()) { *out = &it->second; return GL_OK; }
@@ -291,13 +271,13 @@ static int plan_tables(gl_plan *pl, gl_dev_tables **out) {
       if (st == GL_OK && n <= kFullTwiddleMax && full_twiddles_enabled()) {
         void *p = nullptr;
         cudaError_t e = cudaMalloc(&p, n * sizeof(uint64_t));
-        if (e != cudaSuccess) { st = cuda_status(e); break; }
+        if (e != cudaSuccess) { st = gl_cuda_status(e); break; }
         t.owned.push_back(p);
         t.tw_full[d] = (uint64_t *)p;
         const unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 152 * 32);
         gl_fill_pass_twiddles<<<blocks, 256>>>(t.tw_full[d], t.tw_lo[d], t.tw_hi[d], pl->n1, pl->n2);
         e = cudaDeviceSynchronize();
-        if (e != cudaSuccess) st = cuda_status(e);
+        if (e != cudaSuccess) st = gl_cuda_status(e);
       }
     }
   }
@@ -379,7 +359,7 @@ static std::string kernel_label(const gl_kernel_entry *k, int role) {
 }
 
 // Launch `k` with optional event bracketing.  role: 0 full, 1 col, 2 row.
-static void launch(const gl_kernel_entry *k, int role, const gl_pass_args &a, dim3 grid,
+void gl_launch(const gl_kernel_entry *k, int role, const gl_pass_args &a, dim3 grid,
                    uint64_t elements, cudaStream_t stream) {
   bool on;
   { std::lock_guard<std::mutex> lk(g_prof_mu); on = g_prof_on; }
@@ -407,7 +387,7 @@ extern "C" int gl_profile_read(gl_profile_entry *out, int cap) {
   std::map<std::string, gl_profile_entry> agg;
   for (auto &r : g_prof) {
     cudaError_t e = cudaEventSynchronize(r.b);
-    if (e != cudaSuccess) return -cuda_status(e);
+    if (e != cudaSuccess) return -gl_cuda_status(e);
     float ms = 0;
     cudaEventElapsedTime(&ms, r.a, r.b);
     std::string name = kernel_label(r.k, (int)r.col);
@@ -452,13 +432,13 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
       for (uint64_t b = 0; b < B; b++) {
         cudaError_t e = cudaMemcpyAsync(dst + b * bs, src + b * bs, n * C * sizeof(uint64_t),
                                         cudaMemcpyDeviceToDevice, stream);
-        if (e != cudaSuccess) return cuda_status(e);
+        if (e != cudaSuccess) return gl_cuda_status(e);
       }
     }
     return GL_OK;
   }
   gl_dev_tables *t = nullptr;
-  int st = plan_tables(pl, &t);
+  int st = gl_plan_tables(pl, &t);
   if (st != GL_OK) return st;
   const int d = inv ? 1 : 0;
   const bool coset = lo->itw_lo != nullptr;
@@ -488,7 +468,7 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
         const uint64_t c = std::min(per, B - off);
         a.in = src + off * bs; a.out = dst + off * bs;
         a.lanes = (uint32_t)c;
-        launch(k, 0, a, dim3((unsigned)((c + k->lanes - 1) / k->lanes)), c * n, stream);
+        gl_launch(k, 0, a, dim3((unsigned)((c + k->lanes - 1) / k->lanes)), c * n, stream);
       }
     } else {
       // Lanes are the C interleaved columns; batch items on grid.y.
@@ -500,11 +480,11 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
       for (uint64_t off = 0; off < B; off += kMaxGridYZ) {
         const uint64_t c = std::min(kMaxGridYZ, B - off);
         a.in = src + off * bs; a.out = dst + off * bs;
-        launch(k, 0, a, dim3((unsigned)((C + k->lanes - 1) / k->lanes), (unsigned)c),
+        gl_launch(k, 0, a, dim3((unsigned)((C + k->lanes - 1) / k->lanes), (unsigned)c),
                c * n * C, stream);
       }
     }
-    return cuda_status(cudaGetLastError());
+    return gl_cuda_status(cudaGetLastError());
   }
   // Four-step: n = n1*n2, j = n2*j1 + j2, k = k1 + n1*k2.
   const uint64_t n1 = pl->n1, n2 = pl->n2;
@@ -531,7 +511,7 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
     }
     const uint64_t lanes1 = n2 * C;
     if ((lanes1 + GL_PASS_LANES - 1) / GL_PASS_LANES > 0x7fffffffull) return GL_ERR_INVALID;
-    launch(kc, 1, a, dim3((unsigned)((lanes1 + GL_PASS_LANES - 1) / GL_PASS_LANES), (unsigned)cb),
+    gl_launch(kc, 1, a, dim3((unsigned)((lanes1 + GL_PASS_LANES - 1) / GL_PASS_LANES), (unsigned)cb),
            cb * n * C, stream);
     // ROW: n2-point transforms along j2 for every (k1, c); transposed store.
     gl_pass_args b = base_args();
@@ -543,7 +523,7 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
       b.in_ls = (int64_t)n2; b.in_is = 1; b.out_ls = 1; b.out_is = (int64_t)n1;
       b.in_bs = (int64_t)n; b.out_bs = (int64_t)bs;
       b.lanes = (uint32_t)n1;
-      launch(kr, 2, b, dim3((unsigned)(n1 / GL_PASS_LANES), (unsigned)cb), cb * n, stream);
+      gl_launch(kr, 2, b, dim3((unsigned)(n1 / GL_PASS_LANES), (unsigned)cb), cb * n, stream);
     } else {
       b.in = scratch + off * n * C; b.out = dst + off * bs;
       b.in_ls = 1; b.in_is = (int64_t)C; b.out_ls = 1; b.out_is = (int64_t)(n1 * C);
@@ -551,11 +531,11 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
       b.in_bs2 = (int64_t)(n * C); b.out_bs2 = (int64_t)bs;      // grid.z: batch
       b.flags |= GL_PF_LOAD_LANE_FAST;
       b.lanes = (uint32_t)C;
-      launch(kr, 2, b, dim3((unsigned)((C + GL_PASS_LANES - 1) / GL_PASS_LANES), (unsigned)n1,
+      gl_launch(kr, 2, b, dim3((unsigned)((C + GL_PASS_LANES - 1) / GL_PASS_LANES), (unsigned)n1,
                             (unsigned)cb), cb * n * C, stream);
     }
   }
-  return cuda_status(cudaGetLastError());
+  return gl_cuda_status(cudaGetLastError());
 }
 
 static int run_device(gl_plan *pl, uint64_t *data, uint64_t count, bool inv, uint64_t *scratch,
@@ -563,7 +543,7 @@ static int run_device(gl_plan *pl, uint64_t *data, uint64_t count, bool inv, uin
   return enqueue_transform(pl, data, data, 1, count, pl->size, inv, scratch, stream);
 }
 
-static void init_mempool_once() {
+void gl_init_mempool_once() {
   static std::once_flag once;
   std::call_once(once, [] {
     int dev = 0;
@@ -586,7 +566,7 @@ static int execute(gl_plan *pl, uint64_t *data, uint64_t len, int dir, int mem, 
   const uint64_t count = len / pl->size;
   const bool inv = dir == GL_INVERSE;
   if (pl->kind == 0) return GL_OK;
-  init_mempool_once();
+  gl_init_mempool_once();
   const uint64_t need = gl_plan_workspace_bytes(pl, count);
   int st = GL_OK;
   if (mem == GL_MEM_DEVICE) {
@@ -595,7 +575,7 @@ static int execute(gl_plan *pl, uint64_t *data, uint64_t len, int dir, int mem, 
     if (need && (!ws || ws_bytes < need)) {
       if (ws) return GL_ERR_INVALID;
       cudaError_t e = cudaMallocAsync((void **)&scratch, need, stream);
-      if (e != cudaSuccess) return cuda_status(e);
+      if (e != cudaSuccess) return gl_cuda_status(e);
       own = true;
     }
     st = run_device(pl, data, count, inv, scratch, stream);
@@ -605,7 +585,7 @@ static int execute(gl_plan *pl, uint64_t *data, uint64_t len, int dir, int mem, 
   // Host memory: stage through the device and return when the result is back.
   uint64_t *dbuf = nullptr;
   cudaError_t e = cudaMallocAsync((void **)&dbuf, len * sizeof(uint64_t) + need, stream);
-  if (e != cudaSuccess) return cuda_status(e);
+  if (e != cudaSuccess) return gl_cuda_status(e);
   e = cudaMemcpyAsync(dbuf, data, len * sizeof(uint64_t), cudaMemcpyHostToDevice, stream);
   if (e == cudaSuccess) {
     st = run_device(pl, dbuf, count, inv, need ? dbuf + len : nullptr, stream);
@@ -615,8 +595,8 @@ static int execute(gl_plan *pl, uint64_t *data, uint64_t len, int dir, int mem, 
   cudaFreeAsync(dbuf, stream);
   cudaError_t e2 = cudaStreamSynchronize(stream);
   if (st != GL_OK) return st;
-  if (e != cudaSuccess) return cuda_status(e);
-  return cuda_status(e2);
+  if (e != cudaSuccess) return gl_cuda_status(e);
+  return gl_cuda_status(e2);
 }
 
 extern "C" int gl_plan_execute(const gl_plan *plan, uint64_t *data, uint64_t len, int dir, int mem,
@@ -657,7 +637,7 @@ struct gl_tmp {
   int alloc(size_t bytes, cudaStream_t st) {
     s = st;
     if (bytes == 0) return GL_OK;
-    return cuda_status(cudaMallocAsync(&p, bytes, st));
+    return gl_cuda_status(cudaMallocAsync(&p, bytes, st));
   }
   ~gl_tmp() { if (p) cudaFreeAsync(p, s); }
   uint64_t *u64() { return (uint64_t *)p; }
@@ -674,7 +654,7 @@ extern "C" int gl_ntt_columns(uint64_t *data, uint64_t rows, uint64_t cols, int 
   gl_plan *pl = nullptr;
   int st = gl_plan_create(rows, &pl);
   if (st != GL_OK) return st;
-  init_mempool_once();
+  gl_init_mempool_once();
   const uint64_t len = rows * cols;
   const size_t scratch = pl->kind == 2 ? len * sizeof(uint64_t) : 0;
   if (mem == GL_MEM_DEVICE) {
@@ -687,13 +667,13 @@ extern "C" int gl_ntt_columns(uint64_t *data, uint64_t rows, uint64_t cols, int 
     gl_tmp dbuf;
     if ((st = dbuf.alloc(len * sizeof(uint64_t) + scratch, stream)) != GL_OK) return st;
     cudaError_t e = cudaMemcpyAsync(dbuf.u64(), data, len * 8, cudaMemcpyHostToDevice, stream);
-    if (e != cudaSuccess) return cuda_status(e);
+    if (e != cudaSuccess) return gl_cuda_status(e);
     st = enqueue_transform(pl, dbuf.u64(), dbuf.u64(), cols, 1, len, dir == GL_INVERSE,
                            scratch ? dbuf.u64() + len : nullptr, stream);
     if (st == GL_OK)
-      st = cuda_status(cudaMemcpyAsync(data, dbuf.u64(), len * 8, cudaMemcpyDeviceToHost, stream));
+      st = gl_cuda_status(cudaMemcpyAsync(data, dbuf.u64(), len * 8, cudaMemcpyDeviceToHost, stream));
   }
-  st2 = cuda_status(cudaStreamSynchronize(stream));
+  st2 = gl_cuda_status(cudaStreamSynchronize(stream));
   return st != GL_OK ? st : st2;
 }
 
@@ -705,7 +685,7 @@ static std::map<std::tuple<int, uint64_t, uint64_t>, std::pair<uint64_t *, uint6
 static int coset_tables(uint64_t g, uint64_t n, const uint64_t **lo, const uint64_t **hi) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_status(e);
+  if (e != cudaSuccess) return gl_cuda_status(e);
   std::lock_guard<std::mutex> lk(g_coset_mu);
   auto key = std::make_tuple(dev, g, n);
   auto it = g_coset.find(key);
@@ -747,7 +727,7 @@ static int lde_device(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t co
   uint64_t *coef = tmp.u64(), *scr = tmp.u64() + nc;
   if (n == 1) {
     cudaError_t e = cudaMemcpyAsync(coef, in, nc * 8, cudaMemcpyDeviceToDevice, stream);
-    if (e != cudaSuccess) return cuda_status(e);
+    if (e != cudaSuccess) return gl_cuda_status(e);
   } else if ((st = enqueue_transform(pn, in, coef, cols, 1, nc, true, scr, stream)) != GL_OK) {
     return st;
   }
@@ -757,7 +737,7 @@ static int lde_device(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t co
   lo.itw_hi = chi;
   if (pm->kind == 0) {  // m == 1: the value is the constant coefficient
     cudaError_t e = cudaMemcpyAsync(out, coef, nc * 8, cudaMemcpyDeviceToDevice, stream);
-    return cuda_status(e);
+    return gl_cuda_status(e);
   }
   return enqueue_transform(pm, coef, out, cols, 1, mc, false, scr, stream, &lo);
 }
@@ -768,7 +748,7 @@ extern "C" int gl_coset_lde(const uint64_t *in, uint64_t *out, uint64_t n, uint6
   if (!in || !out || cols == 0 || blowup == 0) return GL_ERR_INVALID;
   if (mem != GL_MEM_HOST && mem != GL_MEM_DEVICE) return GL_ERR_INVALID;
   if (!gl_is_divisor(n) || !gl_is_divisor(n * (uint64_t)blowup)) return GL_ERR_UNSUPPORTED_SIZE;
-  init_mempool_once();
+  gl_init_mempool_once();
   if (mem == GL_MEM_DEVICE) return lde_device(in, out, n, cols, blowup, shift, stream);
   const uint64_t nc = n * cols, mc = nc * blowup;
   int st;
@@ -776,12 +756,12 @@ extern "C" int gl_coset_lde(const uint64_t *in, uint64_t *out, uint64_t n, uint6
     gl_tmp dbuf;
     if ((st = dbuf.alloc((nc + mc) * sizeof(uint64_t), stream)) != GL_OK) return st;
     cudaError_t e = cudaMemcpyAsync(dbuf.u64(), in, nc * 8, cudaMemcpyHostToDevice, stream);
-    if (e != cudaSuccess) return cuda_status(e);
+    if (e != cudaSuccess) return gl_cuda_status(e);
     st = lde_device(dbuf.u64(), dbuf.u64() + nc, n, cols, blowup, shift, stream);
     if (st == GL_OK)
-      st = cuda_status(cudaMemcpyAsync(out, dbuf.u64() + nc, mc * 8, cudaMemcpyDeviceToHost, stream));
+      st = gl_cuda_status(cudaMemcpyAsync(out, dbuf.u64() + nc, mc * 8, cudaMemcpyDeviceToHost, stream));
   }
-  int st2 = cuda_status(cudaStreamSynchronize(stream));
+  int st2 = gl_cuda_status(cudaStreamSynchronize(stream));
   return st != GL_OK ? st : st2;
 }
 

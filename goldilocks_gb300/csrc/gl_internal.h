@@ -4,6 +4,11 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
 #include "gl_pass3.cuh"
 
 typedef void (*gl_launch_fn)(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
@@ -36,3 +41,32 @@ const gl_kernel_entry *gl_find_kernel(uint64_t m, bool full, bool inv);
 
 #define GL_PASS_LANES 4
 #define GL_TW_SPLIT 4096  // two-level pass twiddle: e = hi*4096 + lo
+
+// Device-resident twiddle tables of one plan on one device.
+struct gl_dev_tables {
+  uint64_t *blk[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [stage][dir] omega_m^e
+  uint64_t *blk_scaled_inv = nullptr;                               // FULL inverse: omega^-e / n
+  uint64_t *tw_lo[2] = {nullptr, nullptr};                          // pass twiddle, [dir]
+  uint64_t *tw_hi[2] = {nullptr, nullptr};
+  uint64_t *tw_full[2] = {nullptr, nullptr};  // omega_n^(col*k) at [k*n2 + col], [dir]
+  std::vector<void *> owned;
+};
+
+struct gl_plan {
+  uint64_t size = 0;
+  int kind = 0;                 // 0: no-op (size <= 1), 1: FULL, 2: COL+ROW
+  uint64_t n1 = 0, n2 = 0;      // kind 2: COL over n1, ROW over n2
+  const gl_kernel_entry *k[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [stage][dir]
+  std::string tree;
+  std::mutex mu;
+  std::map<int, gl_dev_tables> dev;  // per device id
+};
+
+// Twiddle tables of `pl` on the current device (built on first use).
+int gl_plan_tables(gl_plan *pl, gl_dev_tables **out);
+// Launch `k` (optionally bracketed by profiling events).  role: 0 full,
+// 1 col, 2 row.
+void gl_launch(const gl_kernel_entry *k, int role, const gl_pass_args &a, dim3 grid,
+               uint64_t elements, cudaStream_t stream);
+int gl_cuda_status(cudaError_t e);
+void gl_init_mempool_once();

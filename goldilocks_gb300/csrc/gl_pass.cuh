@@ -27,6 +27,8 @@ enum : uint32_t {
   GL_PF_STORE_LANE_FAST = 8u,  // adjacent threads take adjacent lanes on store
   GL_PF_IN_TWIDDLE = 16u,      // inputs *= g^(j*itw_jmul + lane / tw_lane_div)
   GL_PF_TW_TABLE = 32u,        // pass twiddle from tw_full[k*tw_ld + lane / tw_lane_div]
+  GL_PF_LOAD_CG = 64u,         // read inputs through L2 only (written in the same launch)
+  GL_PF_PTR_TABLE = 128u,      // batch item by = in_ptrs[by] / out_ptrs[by] (no *_bs)
 };
 
 struct gl_pass_args {
@@ -49,6 +51,8 @@ struct gl_pass_args {
   uint64_t itw_jmul;
   const uint64_t *tw_full;   // full pass-twiddle table omega_n^(col*k) at [k*tw_ld + col]
   int64_t tw_ld;
+  const uint64_t *const *in_ptrs;  // GL_PF_PTR_TABLE: base pointer of batch item by
+  uint64_t *const *out_ptrs;
 };
 
 // Pass twiddle omega_n^(col*k): from the full table when present, else from

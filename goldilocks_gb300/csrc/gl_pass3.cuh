@@ -39,16 +39,20 @@ constexpr size_t gl_p3_smem_bytes() {
                                             : (size_t)LANES * gl_p3_layout<R1, R2, R3>::LS * 8;
 }
 
+// One CTA's work: tile (bx, by, bz) of the pass described by `a`, with NT
+// threads and the dynamic shared memory `sm`.  Called by gl_pass3_kernel
+// (tile = blockIdx) and by the persistent batch kernel (tile from its queue).
 template <int R1, int R2, int R3, int LANES, int NT, bool INV>
-__global__ void __launch_bounds__(NT) gl_pass3_kernel(const gl_pass_args a) {
+__device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int64_t by,
+                                          int64_t bz, uint64_t *sm) {
   using L = gl_p3_layout<R1, R2, R3>;
   constexpr int M = L::M;
   constexpr int S1 = R2 * R3;
-  extern __shared__ uint64_t sm[];
 
-  const int64_t lane0 = (int64_t)blockIdx.x * LANES;
-  const uint64_t *in = a.in + (int64_t)blockIdx.y * a.in_bs + (int64_t)blockIdx.z * a.in_bs2;
-  uint64_t *out = a.out + (int64_t)blockIdx.y * a.out_bs + (int64_t)blockIdx.z * a.out_bs2;
+  const int64_t lane0 = bx * LANES;
+  const bool ptr_table = (a.flags & GL_PF_PTR_TABLE) != 0;
+  const uint64_t *in = ptr_table ? a.in_ptrs[by] + bz * a.in_bs2 : a.in + by * a.in_bs + bz * a.in_bs2;
+  uint64_t *out = ptr_table ? a.out_ptrs[by] + bz * a.out_bs2 : a.out + by * a.out_bs + bz * a.out_bs2;
   const bool scale_all = (a.flags & GL_PF_SCALE_ALL) != 0;
   const bool load_lane_fast = (a.flags & GL_PF_LOAD_LANE_FAST) != 0;
   const bool store_lane_fast = (a.flags & GL_PF_STORE_LANE_FAST) != 0;
@@ -64,10 +68,19 @@ __global__ void __launch_bounds__(NT) gl_pass3_kernel(const gl_pass_args a) {
       const bool live = lane < (int64_t)a.lanes;
       uint64_t x[R1];
       const uint64_t *src = in + lane * a.in_ls + (int64_t)g * a.in_is;
+      if (a.flags & GL_PF_LOAD_CG) {
+        // Input written earlier in the same launch by other CTAs: read via L2.
 #pragma unroll
-      for (int t = 0; t < R1; t++) {
-        const uint32_t j = (uint32_t)(g + S1 * t);
-        x[t] = (live && j < a.in_limit) ? src[(int64_t)(S1 * t) * a.in_is] : 0;
+        for (int t = 0; t < R1; t++) {
+          const uint32_t j = (uint32_t)(g + S1 * t);
+          x[t] = (live && j < a.in_limit) ? __ldcg(src + (int64_t)(S1 * t) * a.in_is) : 0;
+        }
+      } else {
+#pragma unroll
+        for (int t = 0; t < R1; t++) {
+          const uint32_t j = (uint32_t)(g + S1 * t);
+          x[t] = (live && j < a.in_limit) ? src[(int64_t)(S1 * t) * a.in_is] : 0;
+        }
       }
       if (a.flags & GL_PF_IN_TWIDDLE) {
         const uint64_t col = (uint64_t)lane / a.tw_lane_div;
@@ -108,7 +121,7 @@ __global__ void __launch_bounds__(NT) gl_pass3_kernel(const gl_pass_args a) {
     }
   }
   if constexpr (L::NR == 1) return;
-  __syncthreads();
+  __syncthreads();  // uniform: every thread of the CTA reaches it
 
   // ------------------------------------------------------------- round 2
   if constexpr (L::NR == 3) {
@@ -172,4 +185,10 @@ __global__ void __launch_bounds__(NT) gl_pass3_kernel(const gl_pass_args a) {
       }
     }
   }
+}
+
+template <int R1, int R2, int R3, int LANES, int NT, bool INV>
+__global__ void __launch_bounds__(NT) gl_pass3_kernel(const gl_pass_args a) {
+  extern __shared__ uint64_t sm[];
+  gl_block3<R1, R2, R3, LANES, NT, INV>(a, blockIdx.x, blockIdx.y, blockIdx.z, sm);
 }

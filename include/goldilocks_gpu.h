@@ -118,6 +118,32 @@ int gl_ntt_columns(uint64_t *data, uint64_t rows, uint64_t cols, int dir, int me
 int gl_coset_lde(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t cols, uint32_t blowup,
                  uint64_t shift, int mem, void *stream);
 
+/* ---- batches of polynomials of uneven lengths (no counterpart in the reference) ---- */
+
+typedef struct {
+  uint64_t *data;  /* device pointer to the polynomial's values (transformed in place) */
+  uint64_t len;    /* its length: a divisor of p - 1 */
+  int32_t dir;     /* GL_FORWARD or GL_INVERSE */
+  int32_t reserved;
+} gl_poly;
+
+enum { GL_BATCH_AUTO = 0, GL_BATCH_PERSISTENT = 1, GL_BATCH_BUCKETS = 2, GL_BATCH_PER_CALL = 3 };
+
+/* Transform every polynomial of the batch (device memory) on `stream` and
+ * wait for completion.  GL_BATCH_PERSISTENT: one persistent-kernel launch
+ * pulling (polynomial, pass, tile) items from a device queue;
+ * GL_BATCH_BUCKETS: launches per (size, direction) bucket, replayed from a
+ * CUDA graph cached per batch shape; GL_BATCH_PER_CALL: one gl_ntt/gl_intt per
+ * polynomial; GL_BATCH_AUTO: the mode gl_batch_autotune chose for this batch
+ * shape, else persistent.  Sizes the persistent and bucket kernels are not
+ * built for run per call.  Bounded waits: GL_ERR_TIMEOUT if a dependency did
+ * not complete within 2 s. */
+int gl_batch_execute(const gl_poly *polys, uint64_t count, int mode, void *stream);
+/* Time the three explicit modes (`reps` runs each; mean ms written to
+ * ms_out[0..2] when non-null) and remember the fastest for this batch shape.
+ * The polynomials are transformed (1 + reps) times per mode. */
+int gl_batch_autotune(const gl_poly *polys, uint64_t count, int reps, void *stream, double *ms_out);
+
 /* Fill out[0..n) with field elements uniform in [0, p): element i is the
  * first of splitmix64(splitmix64(seed) ^ (offset + i + (k << 48))), k = 0, 1,
  * ..., that is below p.  Host memory; the bench and tests use it for seeded

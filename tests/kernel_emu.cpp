@@ -25,6 +25,7 @@ static std::barrier<> *g_bar = nullptr;
 #define __shared__
 #define __syncthreads() g_bar->arrive_and_wait()
 #define __ldg(p) (*(p))
+#define __ldcg(p) (*(p))
 
 uint64_t sm[1 << 16];  // the CTA's dynamic shared memory
 

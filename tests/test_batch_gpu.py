@@ -1,0 +1,54 @@
+"""GPU parity of batched transforms of uneven lengths: every mode against the
+oracle per polynomial, and the modes against each other at the configured
+batch shape (1024 polynomials, log2 n uniform in [12, 18], half inverse)."""
+import numpy as np
+import pytest
+
+from conftest import from_dev, rand_field, to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def make_batch(cuda, sizes, seed):
+    xs, items = [], []
+    for i, n in enumerate(sizes):
+        x = rand_field(n, seed=seed * 1000 + i)
+        xs.append(x)
+        items.append((to_dev(cuda, x), i % 2))
+    return xs, items
+
+
+@pytest.mark.parametrize("mode_name", ["PERSISTENT", "BUCKETS", "PER_CALL", "AUTO"])
+def test_modes_match_oracle(gl, oracle, cuda, mode_name):
+    from goldilocks_gb300 import batch as B
+    sizes = [4096, 8192, 1 << 16, 64, 4096, 1 << 13, 1 << 18, 1 << 14, 16, 1 << 15, 8192, 2048]
+    xs, items = make_batch(cuda, sizes, seed=3)
+    B.run(items, mode=getattr(B, mode_name))
+    for x, (d, direction) in zip(xs, items):
+        want = oracle.intt(x) if direction else oracle.ntt(x)
+        assert np.array_equal(from_dev(d), want), (len(x), direction)
+
+
+def test_persistent_matches_per_call_config_shape(gl, cuda):
+    """1024 polynomials, log2 n ~ U[12, 18], odd index inverse: persistent and
+    bucketed results are bit-identical to per-call results."""
+    from goldilocks_gb300 import batch as B
+    rng = np.random.default_rng(2024)
+    sizes = [1 << int(k) for k in rng.integers(12, 19, 1024)]
+    outs = {}
+    for mode in (B.PER_CALL, B.PERSISTENT, B.BUCKETS):
+        _, items = make_batch(cuda, sizes, seed=5)
+        B.run(items, mode=mode)
+        outs[mode] = [from_dev(d) for d, _ in items]
+    for a, b, c in zip(outs[B.PER_CALL], outs[B.PERSISTENT], outs[B.BUCKETS]):
+        assert np.array_equal(a, b) and np.array_equal(a, c)
+
+
+def test_autotune_picks_a_mode(gl, cuda):
+    from goldilocks_gb300 import batch as B
+    sizes = [4096, 1 << 14, 1 << 16] * 8
+    _, items = make_batch(cuda, sizes, seed=9)
+    ms = B.autotune(items, reps=2)
+    assert set(ms) == {"persistent", "buckets", "per_call"} and all(v > 0 for v in ms.values())
+    _, items2 = make_batch(cuda, sizes, seed=9)
+    B.run(items2, mode=B.AUTO)
