@@ -37,6 +37,7 @@ SIGNATURES = [
     ("gl_coset_lde", _int, [_vp, _vp, _u64, _u64, _u32, _u64, _int, _vp]),
     ("gl_batch_execute", _int, [_vp, _u64, _int, _vp]),
     ("gl_batch_autotune", _int, [_vp, _u64, _int, _vp, _vp]),
+    ("gl_ntt_noalloc", _int, [_vp, _u64, _int, _vp]),
     ("gl_profile_enable", _int, [_int]),
     ("gl_profile_read", _int, [_vp, _int]),
 ]

@@ -144,6 +144,32 @@ int gl_batch_execute(const gl_poly *polys, uint64_t count, int mode, void *strea
  * The polynomials are transformed (1 + reps) times per mode. */
 int gl_batch_autotune(const gl_poly *polys, uint64_t count, int reps, void *stream, double *ms_out);
 
+/* ---- transform without allocation (no counterpart in the reference) ---- */
+
+/* Longest transform gl_ntt_noalloc accepts: its scratch is a fixed device
+ * array of this many words (8 MiB) that every GPU loading the library keeps
+ * until the process exits. */
+#define GL_NTT_NOALLOC_MAX_LEN (1u << 20)
+
+/* Forward (dir = GL_FORWARD) or inverse transform of the device buffer `data`
+ * in place, on `stream`, without allocating any memory: the intermediate of
+ * the two-pass schedule and the twiddle tables live in fixed device arrays
+ * inside the library.  It exists for callers that cannot allocate device
+ * memory -- for example a worker that must stay within a device-memory budget
+ * another framework has already reserved, or a latency-critical thread that
+ * may not call cudaMalloc (which can synchronise the whole device) -- and
+ * computes exactly what gl_ntt / gl_intt compute.
+ *
+ * Lengths: powers of two from 2^13 to GL_NTT_NOALLOC_MAX_LEN; longer or
+ * non-power-of-two lengths return GL_ERR_INVALID (non-divisors of p - 1:
+ * GL_ERR_UNSUPPORTED_SIZE).  The first call on each device looks up the
+ * device addresses of the fixed arrays (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  All calls share the arrays, so calls
+ * that overlap on the GPU (different streams without ordering) race: order
+ * them on one stream or synchronise between them.  Each call writes every
+ * array word it later reads, so nothing needs clearing between calls. */
+int gl_ntt_noalloc(uint64_t *data, uint64_t len, int dir, void *stream);
+
 /* Fill out[0..n) with field elements uniform in [0, p): element i is the
  * first of splitmix64(splitmix64(seed) ^ (offset + i + (k << 48))), k = 0, 1,
  * ..., that is below p.  Host memory; the bench and tests use it for seeded
