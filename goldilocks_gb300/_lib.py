@@ -37,6 +37,14 @@ SIGNATURES = [
     ("gl_coset_lde", _int, [_vp, _vp, _u64, _u64, _u32, _u64, _int, _vp]),
     ("gl_batch_execute", _int, [_vp, _u64, _int, _vp]),
     ("gl_batch_autotune", _int, [_vp, _u64, _int, _vp, _vp]),
+    ("gl_server_create", _int, [_u64, _int, _int, ctypes.POINTER(_vp)]),
+    ("gl_server_request_bytes", _int, [_vp, ctypes.POINTER(_u64)]),
+    ("gl_server_submit", _int, [_vp, _vp, ctypes.POINTER(_u64)]),
+    ("gl_server_poll", _int, [_vp, _u64, ctypes.POINTER(_int)]),
+    ("gl_server_wait", _int, [_vp, _u64, _int, ctypes.POINTER(_int)]),
+    ("gl_server_cancel", _int, [_vp, _u64]),
+    ("gl_server_get_stats", _int, [_vp, _vp]),
+    ("gl_server_destroy", _int, [_vp]),
     ("gl_ntt_noalloc", _int, [_vp, _u64, _int, _vp]),
     ("gl_profile_enable", _int, [_int]),
     ("gl_profile_read", _int, [_vp, _int]),
@@ -49,6 +57,22 @@ class Poly(ctypes.Structure):
 
 
 GL_BATCH_AUTO, GL_BATCH_PERSISTENT, GL_BATCH_BUCKETS, GL_BATCH_PER_CALL = 0, 1, 2, 3
+
+
+GL_OP_NTT, GL_OP_INTT, GL_OP_LDE = 0, 1, 2
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("op", ctypes.c_int32), ("reserved", ctypes.c_int32), ("n", ctypes.c_uint64),
+                ("cols", ctypes.c_uint64), ("inp", ctypes.c_void_p), ("out", ctypes.c_void_p),
+                ("blowup", ctypes.c_uint32), ("reserved2", ctypes.c_uint32), ("shift", ctypes.c_uint64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("rejected", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+                ("elements", ctypes.c_uint64), ("max_in_use_bytes", ctypes.c_uint64),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double)]
 
 
 class ProfileEntry(ctypes.Structure):

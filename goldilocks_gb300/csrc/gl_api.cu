@@ -196,6 +196,36 @@ static void choose_schedule(gl_plan *pl) {
     }
     return;
   }
+  // Three passes for n beyond 4096^2: n = n1*n2*n3, all with pass kernels,
+  // the largest factor as small as possible.
+  uint64_t b1 = 0, b2 = 0;
+  for (uint64_t n1 : divisor_list()) {
+    if (n1 > 4096) break;
+    if (n % n1 || !pass_size_ok(n1) || n1 % GL_PASS_LANES) continue;
+    const uint64_t r = n / n1;
+    for (uint64_t n2 : divisor_list()) {
+      if (n2 > 4096) break;
+      if (r % n2 || !pass_size_ok(n2) || !pass_size_ok(r / n2) || n2 % GL_PASS_LANES ||
+          (r / n2) % GL_PASS_LANES)
+        continue;
+      const uint64_t n3 = r / n2;
+      const uint64_t worst = std::max(n1, std::max(n2, n3));
+      if (b1 == 0 || worst < std::max(b1, std::max(b2, n / (b1 * b2))))
+        { b1 = n1; b2 = n2; }
+    }
+  }
+  if (b1) {
+    pl->kind = 3;
+    pl->n1 = b1;
+    pl->n2 = b2;
+    pl->n3 = n / (b1 * b2);
+    for (int d = 0; d < 2; d++) {
+      pl->k[0][d] = gl_find_kernel(pl->n1, false, d == 1);
+      pl->k[1][d] = gl_find_kernel(pl->n2, false, d == 1);
+      pl->k[2][d] = gl_find_kernel(pl->n3, false, d == 1);
+    }
+    return;
+  }
   pl->kind = -1;  // divisor without a GPU schedule
 }
 
@@ -280,6 +310,23 @@ int gl_plan_tables(gl_plan *pl, gl_dev_tables **out) {
         if (e != cudaSuccess) st = gl_cuda_status(e);
       }
     }
+  } else if (pl->kind == 3) {
+    const uint64_t n23 = pl->n2 * pl->n3;
+    for (int d = 0; d < 2 && st == GL_OK; d++) {
+      st = upload(t, powers(h_root(pl->n1, d), pl->n1, 1), &t.blk[0][d]);
+      if (st == GL_OK) st = upload(t, powers(h_root(pl->n2, d), pl->n2, 1), &t.blk[1][d]);
+      if (st == GL_OK) st = upload(t, powers(h_root(pl->n3, d), pl->n3, 1), &t.blk3[d]);
+      const uint64_t w = h_root(n, d);
+      const uint64_t scale = d ? gl_inv(n % GL_P) : 1;
+      if (st == GL_OK) st = upload(t, powers(w, GL_TW_SPLIT, scale), &t.tw_lo[d]);
+      if (st == GL_OK)
+        st = upload(t, powers(gl_pow(w, GL_TW_SPLIT), (n + GL_TW_SPLIT - 1) / GL_TW_SPLIT, 1), &t.tw_hi[d]);
+      const uint64_t w23 = h_root(n23, d);
+      if (st == GL_OK) st = upload(t, powers(w23, GL_TW_SPLIT, 1), &t.tw23_lo[d]);
+      if (st == GL_OK)
+        st = upload(t, powers(gl_pow(w23, GL_TW_SPLIT), (n23 + GL_TW_SPLIT - 1) / GL_TW_SPLIT, 1),
+                    &t.tw23_hi[d]);
+    }
   }
   if (st != GL_OK) {
     for (void *p : t.owned) cudaFree(p);
@@ -329,7 +376,10 @@ extern "C" int gl_plan_describe(const gl_plan *plan, char *buf, size_t cap) {
   auto kname = [](const gl_kernel_entry *k) { return kernel_shape(k); };
   if (plan->kind == 0) s += "no-op";
   else if (plan->kind == 1) s += "full " + kname(plan->k[0][0]);
-  else s += "col " + kname(plan->k[0][0]) + " + row " + kname(plan->k[1][0]);
+  else if (plan->kind == 2) s += "col " + kname(plan->k[0][0]) + " + row " + kname(plan->k[1][0]);
+  else
+    s += "col " + kname(plan->k[0][0]) + " + col " + kname(plan->k[1][0]) + " + row " +
+         kname(plan->k[2][0]);
   size_t n = std::min(cap - 1, s.size());
   memcpy(buf, s.data(), n);
   buf[n] = 0;
@@ -337,7 +387,7 @@ extern "C" int gl_plan_describe(const gl_plan *plan, char *buf, size_t cap) {
 }
 
 extern "C" uint64_t gl_plan_workspace_bytes(const gl_plan *plan, uint64_t count) {
-  if (!plan || plan->kind != 2) return 0;
+  if (!plan || plan->kind < 2) return 0;
   return plan->size * count * sizeof(uint64_t);
 }
 
@@ -482,6 +532,68 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
         a.in = src + off * bs; a.out = dst + off * bs;
         gl_launch(k, 0, a, dim3((unsigned)((C + k->lanes - 1) / k->lanes), (unsigned)c),
                c * n * C, stream);
+      }
+    }
+    return gl_cuda_status(cudaGetLastError());
+  }
+  if (pl->kind == 3) {
+    // Three passes, n = n1*n2*n3, j = n2 n3 j1 + n3 j2 + j3,
+    // k = k1 + n1 k2 + n1 n2 k3:
+    //   A  n1-point over j1, times omega_n^(j23 k1)           src -> scratch
+    //   B  per k1: n2-point over j2, times omega_(n2 n3)^(j3 k2)  in place
+    //   C  per (k1, k2): n3-point over j3, stored at k         scratch -> dst
+    // (a column pass writes exactly the positions it reads, so B is in place).
+    const uint64_t n1 = pl->n1, n2 = pl->n2, n3 = pl->n3, n23 = n2 * n3;
+    const gl_kernel_entry *ka = pl->k[0][d], *kb = pl->k[1][d], *kcr = pl->k[2][d];
+    for (uint64_t b = 0; b < B; b++) {
+      const uint64_t *in = src + b * bs;
+      uint64_t *out = dst + b * bs;
+      uint64_t *s1 = scratch + b * n * C;
+      gl_pass_args a = base_args();
+      a.in = in; a.out = s1;
+      a.in_ls = a.out_ls = 1; a.in_is = a.out_is = (int64_t)(n23 * C);
+      a.lanes = (uint32_t)(n23 * C);
+      a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
+      a.tw_m = a.tw_r2 = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
+      a.tw_lane_div = (uint32_t)C;
+      if (coset) {
+        a.flags |= GL_PF_IN_TWIDDLE;
+        a.itw_lo = lo->itw_lo; a.itw_hi = lo->itw_hi; a.itw_jmul = n23;
+      }
+      const uint64_t ta = (n23 * C + GL_PASS_LANES - 1) / GL_PASS_LANES;
+      if (ta > 0x7fffffffull) return GL_ERR_INVALID;
+      gl_launch(ka, 1, a, dim3((unsigned)ta), n * C, stream);
+      gl_pass_args bb = base_args();
+      bb.in_limit = 0xffffffffu;
+      bb.in = s1; bb.out = s1;
+      bb.in_ls = bb.out_ls = 1; bb.in_is = bb.out_is = (int64_t)(n3 * C);
+      bb.in_bs = bb.out_bs = (int64_t)(n23 * C);
+      bb.lanes = (uint32_t)(n3 * C);
+      bb.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
+      bb.tw_m = bb.tw_r2 = t->blk[1][d]; bb.tw_lo = t->tw23_lo[d]; bb.tw_hi = t->tw23_hi[d];
+      bb.tw_lane_div = (uint32_t)C;
+      gl_launch(kb, 1, bb, dim3((unsigned)((n3 * C + GL_PASS_LANES - 1) / GL_PASS_LANES), (unsigned)n1),
+                n * C, stream);
+      gl_pass_args c = base_args();
+      c.in_limit = 0xffffffffu;
+      c.tw_m = c.tw_r2 = t->blk3[d];
+      c.flags = GL_PF_STORE_LANE_FAST;
+      c.in = s1; c.out = out;
+      if (C == 1) {
+        c.in_ls = (int64_t)n3; c.in_is = 1;                       // lanes: rows k2 of block k1
+        c.out_ls = (int64_t)n1; c.out_is = (int64_t)(n1 * n2);
+        c.in_bs = (int64_t)n23; c.out_bs = 1;                     // grid.y: k1
+        c.lanes = (uint32_t)n2;
+        gl_launch(kcr, 2, c, dim3((unsigned)(n2 / GL_PASS_LANES), (unsigned)n1), n, stream);
+      } else {
+        c.in_ls = 1; c.in_is = (int64_t)C;                        // lanes: columns
+        c.out_ls = 1; c.out_is = (int64_t)(n1 * n2 * C);
+        c.in_bs = (int64_t)(n3 * C); c.out_bs = (int64_t)(n1 * C);      // grid.y: k2
+        c.in_bs2 = (int64_t)(n23 * C); c.out_bs2 = (int64_t)C;          // grid.z: k1
+        c.flags |= GL_PF_LOAD_LANE_FAST;
+        c.lanes = (uint32_t)C;
+        gl_launch(kcr, 2, c, dim3((unsigned)((C + GL_PASS_LANES - 1) / GL_PASS_LANES), (unsigned)n2,
+                                  (unsigned)n1), n * C, stream);
       }
     }
     return gl_cuda_status(cudaGetLastError());
@@ -656,7 +768,7 @@ extern "C" int gl_ntt_columns(uint64_t *data, uint64_t rows, uint64_t cols, int 
   if (st != GL_OK) return st;
   gl_init_mempool_once();
   const uint64_t len = rows * cols;
-  const size_t scratch = pl->kind == 2 ? len * sizeof(uint64_t) : 0;
+  const size_t scratch = pl->kind >= 2 ? len * sizeof(uint64_t) : 0;
   if (mem == GL_MEM_DEVICE) {
     gl_tmp tmp;
     if ((st = tmp.alloc(scratch, stream)) != GL_OK) return st;
@@ -717,11 +829,12 @@ static int lde_device(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t co
   // The forward pass reads only the first n rows of the zero-padded input: in
   // the four-step view j = n2*j1 + j2 that is j1 < n / n2, so n2 must divide n.
   if (pm->kind == 2 && n % pm->n2 != 0) return GL_ERR_UNSUPPORTED_SIZE;
+  if (pm->kind == 3 && n % (pm->n2 * pm->n3) != 0) return GL_ERR_UNSUPPORTED_SIZE;
   const uint64_t *clo = nullptr, *chi = nullptr;
   if ((st = coset_tables(shift % GL_P, n, &clo, &chi)) != GL_OK) return st;
   // Coefficients (n x cols) plus scratch for the larger of the two transforms.
   const uint64_t nc = n * cols, mc = m * cols;
-  const uint64_t scratch_words = std::max(pn->kind == 2 ? nc : 0, pm->kind == 2 ? mc : 0);
+  const uint64_t scratch_words = std::max(pn->kind >= 2 ? nc : 0, pm->kind >= 2 ? mc : 0);
   gl_tmp tmp;
   if ((st = tmp.alloc((nc + scratch_words) * sizeof(uint64_t), stream)) != GL_OK) return st;
   uint64_t *coef = tmp.u64(), *scr = tmp.u64() + nc;
@@ -732,7 +845,7 @@ static int lde_device(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t co
     return st;
   }
   gl_load_opts lo;
-  lo.in_limit = (uint32_t)(pm->kind == 2 ? n / pm->n2 : n);
+  lo.in_limit = (uint32_t)(pm->kind == 2 ? n / pm->n2 : pm->kind == 3 ? n / (pm->n2 * pm->n3) : n);
   lo.itw_lo = clo;
   lo.itw_hi = chi;
   if (pm->kind == 0) {  // m == 1: the value is the constant coefficient

@@ -203,8 +203,12 @@ struct dev_block {
 
 int run_per_call(const gl_poly *polys, uint64_t count, cudaStream_t stream, bool sync = true);
 
-int run_persistent(const gl_poly *polys, uint64_t count, const std::vector<poly_plan> &pp,
-                   cudaStream_t stream) {
+// Queue the batch on `stream` without waiting.  The kernel's error word is
+// copied to *err_out (host-pinned or device memory the caller owns) after the
+// kernel; 0 means success.  Polynomials the persistent kernel has no shape for
+// are queued as plain calls first.
+int enqueue_persistent(const gl_poly *polys, uint64_t count, const std::vector<poly_plan> &pp,
+                       cudaStream_t stream, uint32_t *err_out) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -262,7 +266,7 @@ int run_persistent(const gl_poly *polys, uint64_t count, const std::vector<poly_
     }
   }
   while (!pending.empty()) { push_rows(pending.front().first); pending.pop_front(); }
-  if (items.empty()) return gl_cuda_status(cudaStreamSynchronize(stream));
+  if (items.empty()) return gl_cuda_status(cudaMemsetAsync(err_out, 0, sizeof(uint32_t), stream));
 
   // One device block: args | items | counters (head, err, done[count]) | scratch.
   const size_t args_bytes = 2 * count * sizeof(gl_pass_args);
@@ -297,11 +301,23 @@ int run_persistent(const gl_poly *polys, uint64_t count, const std::vector<poly_
                                                (const gl_pass_args *)base, ctr, ctr + 2, ctr + 1,
                                                2000000000ull /* 2 s */);
   if ((e = cudaGetLastError()) != cudaSuccess) return gl_cuda_status(e);
-  uint32_t err = 0;
-  if ((e = cudaMemcpyAsync(&err, ctr + 1, sizeof(err), cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
-    return gl_cuda_status(e);
-  if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return gl_cuda_status(e);
-  return err ? (int)err : GL_OK;
+  e = cudaMemcpyAsync(err_out, ctr + 1, sizeof(uint32_t), cudaMemcpyDefault, stream);
+  return gl_cuda_status(e);
+}
+
+int run_persistent(const gl_poly *polys, uint64_t count, const std::vector<poly_plan> &pp,
+                   cudaStream_t stream) {
+  uint32_t *err = nullptr;
+  cudaError_t e = cudaMallocHost(&err, sizeof(uint32_t));
+  if (e != cudaSuccess) return gl_cuda_status(e);
+  *err = 0;
+  int st = enqueue_persistent(polys, count, pp, stream, err);
+  cudaError_t e2 = cudaStreamSynchronize(stream);
+  const uint32_t v = *err;
+  cudaFreeHost(err);
+  if (st != GL_OK) return st;
+  if (e2 != cudaSuccess) return gl_cuda_status(e2);
+  return v ? (int)v : GL_OK;
 }
 
 // --------------------------------------------------------------- buckets
@@ -322,8 +338,14 @@ int run_buckets(const gl_poly *polys, uint64_t count, const std::vector<poly_pla
                 cudaStream_t stream) {
   // Group by (len, dir); order within a bucket = input order.
   std::map<std::pair<uint64_t, int>, std::vector<uint64_t>> buckets;
-  for (uint64_t i = 0; i < count; i++)
-    if (pp[i].pl->kind > 0) buckets[{polys[i].len, polys[i].dir}].push_back(i);
+  for (uint64_t i = 0; i < count; i++) {
+    if (pp[i].pl->kind == 3) {  // three-pass sizes run as plain calls
+      int st = run_per_call(&polys[i], 1, stream, false);
+      if (st != GL_OK) return st;
+    } else if (pp[i].pl->kind > 0) {
+      buckets[{polys[i].len, polys[i].dir}].push_back(i);
+    }
+  }
   std::vector<std::pair<uint64_t, int>> sig;
   std::vector<uint64_t> order;
   for (auto &kv : buckets)
@@ -430,6 +452,15 @@ std::vector<std::pair<uint64_t, int>> batch_shape(const gl_poly *polys, uint64_t
 }
 
 }  // namespace
+
+// Internal, for the server: queue a persistent batch without waiting.
+int gl_batch_enqueue_persistent(const gl_poly *polys, uint64_t count, cudaStream_t stream,
+                                uint32_t *err_out) {
+  std::vector<poly_plan> pp;
+  int st = resolve(polys, count, pp);
+  if (st != GL_OK) return st;
+  return enqueue_persistent(polys, count, pp, stream, err_out);
+}
 
 extern "C" int gl_batch_execute(const gl_poly *polys, uint64_t count, int mode, void *stream_) {
   cudaStream_t stream = (cudaStream_t)stream_;

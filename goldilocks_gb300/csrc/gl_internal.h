@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/goldilocks_gpu.h"
 #include "gl_pass3.cuh"
 
 typedef void (*gl_launch_fn)(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
@@ -49,14 +50,19 @@ struct gl_dev_tables {
   uint64_t *tw_lo[2] = {nullptr, nullptr};                          // pass twiddle, [dir]
   uint64_t *tw_hi[2] = {nullptr, nullptr};
   uint64_t *tw_full[2] = {nullptr, nullptr};  // omega_n^(col*k) at [k*n2 + col], [dir]
+  // kind 3 only: block table of n3 and the two-level table of omega_(n2*n3).
+  uint64_t *blk3[2] = {nullptr, nullptr};
+  uint64_t *tw23_lo[2] = {nullptr, nullptr};
+  uint64_t *tw23_hi[2] = {nullptr, nullptr};
   std::vector<void *> owned;
 };
 
 struct gl_plan {
   uint64_t size = 0;
-  int kind = 0;                 // 0: no-op (size <= 1), 1: FULL, 2: COL+ROW
-  uint64_t n1 = 0, n2 = 0;      // kind 2: COL over n1, ROW over n2
-  const gl_kernel_entry *k[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [stage][dir]
+  int kind = 0;  // 0: no-op (size <= 1), 1: FULL, 2: COL+ROW, 3: COL+COL+ROW
+  uint64_t n1 = 0, n2 = 0;  // kind 2: COL over n1, ROW over n2
+  uint64_t n3 = 0;          // kind 3: COL over n1, COL over n2 (per k1), ROW over n3
+  const gl_kernel_entry *k[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};  // [stage][dir]
   std::string tree;
   std::mutex mu;
   std::map<int, gl_dev_tables> dev;  // per device id
@@ -70,3 +76,8 @@ void gl_launch(const gl_kernel_entry *k, int role, const gl_pass_args &a, dim3 g
                uint64_t elements, cudaStream_t stream);
 int gl_cuda_status(cudaError_t e);
 void gl_init_mempool_once();
+
+// Queue a batch on the persistent kernel without waiting; the kernel's error
+// word (0 = success) is copied to *err_out afterwards.  (gl_batch.cu)
+int gl_batch_enqueue_persistent(const gl_poly *polys, uint64_t count, cudaStream_t stream,
+                                uint32_t *err_out);

@@ -1,0 +1,343 @@
+// Continuous-batching request server for NTT / inverse NTT / coset LDE jobs
+// on device-resident data (no counterpart in the reference).
+//
+// Requests are queued by gl_server_submit from any thread.  A scheduler
+// thread admits queued requests in arrival order while the device memory they
+// need (the temporaries the server allocates: scratch, LDE coefficients) fits
+// the budget, groups the admitted ones into a batch and launches it on a free
+// slot -- one CUDA stream per slot -- so batches run concurrently on the GPU:
+//   * single-column NTT/iNTT jobs of the batch go to one persistent-kernel
+//     launch (gl_batch.cu); sizes it is not built for run as plain calls;
+//   * multi-column jobs run as column-batched transforms (gl_ntt_columns path);
+//   * LDE jobs run gl_coset_lde.
+// A host function queued after the batch on its stream marks completion;
+// memory returns to the budget and waiters wake.  Requests that arrive while
+// batches are in flight are admitted as slots and memory free up.  Every wait
+// is bounded (gl_server_wait's timeout); a persistent-kernel timeout surfaces
+// as GL_ERR_TIMEOUT on the affected requests.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "../../include/goldilocks_gpu.h"
+#include "gl_internal.h"
+
+namespace {
+
+using clk = std::chrono::steady_clock;
+
+struct job {
+  uint64_t id;
+  gl_request req;
+  uint64_t bytes;           // budgeted device bytes
+  clk::time_point t_submit;
+  clk::time_point t_done;
+  int status = GL_ERR_BUSY;  // GL_ERR_BUSY while pending
+  bool launched = false;
+};
+
+struct slot {
+  cudaStream_t stream = nullptr;
+  bool busy = false;
+  std::vector<std::shared_ptr<job>> jobs;
+  uint32_t *err = nullptr;  // pinned: persistent kernel error word
+  int launch_status = GL_OK;
+};
+
+}  // namespace
+
+struct gl_server {
+  uint64_t budget = 0;
+  uint64_t in_use = 0;
+  uint64_t max_in_use = 0;
+  int max_batch = 64;
+  std::vector<slot> slots;
+  std::mutex mu;
+  std::condition_variable cv;       // scheduler wake-ups
+  std::condition_variable done_cv;  // waiter wake-ups
+  std::deque<std::shared_ptr<job>> queue;
+  std::map<uint64_t, std::shared_ptr<job>> jobs;
+  uint64_t next_id = 1;
+  bool stop = false;
+  std::thread worker;
+  int device = 0;
+  // statistics
+  uint64_t submitted = 0, completed = 0, rejected = 0, batches = 0, elements = 0;
+  std::vector<double> latencies_ms;
+};
+
+namespace {
+
+uint64_t out_rows(const gl_request &r) { return r.op == GL_OP_LDE ? r.n * r.blowup : r.n; }
+
+// Device bytes the server allocates for the request (its temporaries).
+int footprint(const gl_request &r, uint64_t *bytes) {
+  if (r.cols == 0 || (!r.in && r.n) || (!r.out && r.n)) return GL_ERR_INVALID;
+  if (r.op != GL_OP_NTT && r.op != GL_OP_INTT && r.op != GL_OP_LDE) return GL_ERR_INVALID;
+  if (!gl_is_divisor(r.n)) return GL_ERR_UNSUPPORTED_SIZE;
+  if (r.op == GL_OP_LDE) {
+    if (r.blowup == 0) return GL_ERR_INVALID;
+    if (!gl_is_divisor(r.n * (uint64_t)r.blowup)) return GL_ERR_UNSUPPORTED_SIZE;
+    // coefficients (n x cols) + scratch of the larger transform (blowup*n x cols)
+    *bytes = (r.n + r.n * (uint64_t)r.blowup) * r.cols * 8;
+  } else {
+    *bytes = r.n * r.cols * 8;  // scratch of a two- or three-pass transform
+  }
+  return GL_OK;
+}
+
+void CUDART_CB on_batch_done(void *arg);
+
+struct done_ctx {
+  gl_server *srv;
+  int slot;
+};
+
+// Launch one batch on slot `si` (called with the lock released).
+int launch_batch(gl_server *s, int si, std::vector<std::shared_ptr<job>> &batch) {
+  slot &sl = s->slots[si];
+  cudaStream_t st = sl.stream;
+  std::vector<gl_poly> polys;
+  int rc = GL_OK;
+  for (auto &j : batch) {
+    const gl_request &r = j->req;
+    if (r.op == GL_OP_LDE) {
+      rc = gl_coset_lde(r.in, r.out, r.n, r.cols, r.blowup, r.shift, GL_MEM_DEVICE, st);
+    } else {
+      const uint64_t words = r.n * r.cols;
+      if (r.out != r.in) {
+        cudaError_t e = cudaMemcpyAsync(r.out, r.in, words * 8, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) rc = gl_cuda_status(e);
+      }
+      if (rc == GL_OK) {
+        if (r.cols == 1) {
+          polys.push_back({r.out, r.n, r.op == GL_OP_INTT ? GL_INVERSE : GL_FORWARD, 0});
+        } else if (!(r.op == GL_OP_INTT && r.n == 1)) {
+          rc = gl_ntt_columns(r.out, r.n, r.cols, r.op == GL_OP_INTT ? GL_INVERSE : GL_FORWARD,
+                              GL_MEM_DEVICE, st);
+        }
+      }
+    }
+    if (rc != GL_OK) break;
+  }
+  *sl.err = 0;
+  if (rc == GL_OK && !polys.empty())
+    rc = gl_batch_enqueue_persistent(polys.data(), polys.size(), st, sl.err);
+  sl.launch_status = rc;
+  done_ctx *ctx = new done_ctx{s, si};
+  cudaError_t e = cudaLaunchHostFunc(st, on_batch_done, ctx);
+  if (e != cudaSuccess) {
+    delete ctx;
+    return gl_cuda_status(e);
+  }
+  return GL_OK;
+}
+
+void finish_slot(gl_server *s, int si) {
+  // lock held
+  slot &sl = s->slots[si];
+  const int status = sl.launch_status != GL_OK ? sl.launch_status : (*sl.err ? (int)*sl.err : GL_OK);
+  const auto now = clk::now();
+  for (auto &j : sl.jobs) {
+    j->status = status;
+    j->t_done = now;
+    s->in_use -= j->bytes;
+    s->completed++;
+    s->elements += j->req.n * j->req.cols;
+    s->latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - j->t_submit).count());
+  }
+  sl.jobs.clear();
+  sl.busy = false;
+}
+
+void CUDART_CB on_batch_done(void *arg) {
+  // Runs on a CUDA runtime thread: no CUDA calls here.
+  done_ctx *ctx = (done_ctx *)arg;
+  gl_server *s = ctx->srv;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    finish_slot(s, ctx->slot);
+  }
+  delete ctx;
+  s->cv.notify_all();
+  s->done_cv.notify_all();
+}
+
+void scheduler(gl_server *s) {
+  cudaSetDevice(s->device);
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
+    // Find a free slot and the jobs to admit.
+    int free_slot = -1;
+    for (size_t i = 0; i < s->slots.size(); i++)
+      if (!s->slots[i].busy) { free_slot = (int)i; break; }
+    std::vector<std::shared_ptr<job>> batch;
+    if (free_slot >= 0) {
+      while (!s->queue.empty() && (int)batch.size() < s->max_batch) {
+        auto &j = s->queue.front();
+        if (j->status == GL_ERR_CANCELLED) { s->queue.pop_front(); continue; }
+        if (s->in_use + j->bytes > s->budget) break;  // arrival order: wait for memory
+        s->in_use += j->bytes;
+        s->max_in_use = std::max(s->max_in_use, s->in_use);
+        j->launched = true;
+        batch.push_back(j);
+        s->queue.pop_front();
+      }
+    }
+    if (!batch.empty()) {
+      slot &sl = s->slots[free_slot];
+      sl.busy = true;
+      sl.jobs = batch;
+      s->batches++;
+      lk.unlock();
+      int rc = launch_batch(s, free_slot, batch);
+      lk.lock();
+      if (rc != GL_OK) {  // no completion callback was queued
+        sl.launch_status = rc;
+        *sl.err = 0;
+        finish_slot(s, free_slot);
+        s->done_cv.notify_all();
+      }
+      continue;
+    }
+    bool idle = true;
+    for (auto &sl : s->slots) idle = idle && !sl.busy;
+    if (s->stop && s->queue.empty() && idle) break;
+    s->cv.wait_for(lk, std::chrono::milliseconds(50));
+  }
+}
+
+}  // namespace
+
+extern "C" int gl_server_create(uint64_t budget_bytes, int slots, int max_batch, gl_server **out) {
+  if (!out || slots <= 0 || max_batch <= 0 || budget_bytes == 0) return GL_ERR_INVALID;
+  *out = nullptr;
+  gl_server *s = new gl_server();
+  s->budget = budget_bytes;
+  s->max_batch = max_batch;
+  cudaError_t e = cudaGetDevice(&s->device);
+  if (e != cudaSuccess) { delete s; return gl_cuda_status(e); }
+  gl_init_mempool_once();
+  s->slots.resize(slots);
+  for (auto &sl : s->slots) {
+    e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocHost(&sl.err, sizeof(uint32_t));
+    if (e != cudaSuccess) {
+      for (auto &x : s->slots) {
+        if (x.stream) cudaStreamDestroy(x.stream);
+        if (x.err) cudaFreeHost(x.err);
+      }
+      delete s;
+      return gl_cuda_status(e);
+    }
+    *sl.err = 0;
+  }
+  s->worker = std::thread(scheduler, s);
+  *out = s;
+  return GL_OK;
+}
+
+extern "C" int gl_server_request_bytes(const gl_request *req, uint64_t *bytes) {
+  if (!req || !bytes) return GL_ERR_INVALID;
+  return footprint(*req, bytes);
+}
+
+extern "C" int gl_server_submit(gl_server *s, const gl_request *req, uint64_t *id) {
+  if (!s || !req || !id) return GL_ERR_INVALID;
+  uint64_t bytes = 0;
+  int st = footprint(*req, &bytes);
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (st == GL_OK && bytes > s->budget) st = GL_ERR_BUDGET;
+  if (st != GL_OK) {
+    s->rejected++;
+    return st;
+  }
+  auto j = std::make_shared<job>();
+  j->id = s->next_id++;
+  j->req = *req;
+  j->bytes = bytes;
+  j->t_submit = clk::now();
+  s->jobs[j->id] = j;
+  s->queue.push_back(j);
+  s->submitted++;
+  *id = j->id;
+  s->cv.notify_all();
+  return GL_OK;
+}
+
+extern "C" int gl_server_poll(gl_server *s, uint64_t id, int *status) {
+  if (!s || !status) return GL_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(id);
+  if (it == s->jobs.end()) return GL_ERR_NOT_FOUND;
+  *status = it->second->status;
+  return GL_OK;
+}
+
+extern "C" int gl_server_wait(gl_server *s, uint64_t id, int timeout_ms, int *status) {
+  if (!s || !status) return GL_ERR_INVALID;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(id);
+  if (it == s->jobs.end()) return GL_ERR_NOT_FOUND;
+  std::shared_ptr<job> j = it->second;
+  const bool done = s->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms),
+                                        [&] { return j->status != GL_ERR_BUSY; });
+  if (!done) return GL_ERR_TIMEOUT;
+  *status = j->status;
+  s->jobs.erase(id);  // the result has been delivered
+  return GL_OK;
+}
+
+extern "C" int gl_server_cancel(gl_server *s, uint64_t id) {
+  if (!s) return GL_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(id);
+  if (it == s->jobs.end()) return GL_ERR_NOT_FOUND;
+  if (it->second->launched || it->second->status != GL_ERR_BUSY) return GL_ERR_BUSY;
+  it->second->status = GL_ERR_CANCELLED;  // dropped by the scheduler
+  s->done_cv.notify_all();
+  return GL_OK;
+}
+
+extern "C" int gl_server_get_stats(gl_server *s, gl_server_stats *out) {
+  if (!s || !out) return GL_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  out->submitted = s->submitted;
+  out->completed = s->completed;
+  out->rejected = s->rejected;
+  out->batches = s->batches;
+  out->elements = s->elements;
+  out->max_in_use_bytes = s->max_in_use;
+  std::vector<double> v = s->latencies_ms;
+  std::sort(v.begin(), v.end());
+  auto q = [&](double f) { return v.empty() ? 0.0 : v[std::min(v.size() - 1, (size_t)(f * v.size()))]; };
+  out->p50_ms = q(0.50);
+  out->p99_ms = q(0.99);
+  out->max_ms = v.empty() ? 0.0 : v.back();
+  return GL_OK;
+}
+
+extern "C" int gl_server_destroy(gl_server *s) {
+  if (!s) return GL_ERR_INVALID;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv.notify_all();
+  if (s->worker.joinable()) s->worker.join();  // drains the queue and in-flight batches
+  for (auto &sl : s->slots) {
+    cudaStreamSynchronize(sl.stream);
+    cudaStreamDestroy(sl.stream);
+    cudaFreeHost(sl.err);
+  }
+  delete s;
+  return GL_OK;
+}

@@ -144,6 +144,52 @@ int gl_batch_execute(const gl_poly *polys, uint64_t count, int mode, void *strea
  * The polynomials are transformed (1 + reps) times per mode. */
 int gl_batch_autotune(const gl_poly *polys, uint64_t count, int reps, void *stream, double *ms_out);
 
+/* ---- continuous-batching request server (no counterpart in the reference) ---- */
+
+enum { GL_OP_NTT = 0, GL_OP_INTT = 1, GL_OP_LDE = 2 };
+
+typedef struct {
+  int32_t op;          /* GL_OP_NTT, GL_OP_INTT or GL_OP_LDE */
+  int32_t reserved;
+  uint64_t n;          /* rows: the transform length (a divisor of p - 1) */
+  uint64_t cols;       /* columns of the row-major n x cols matrix (>= 1) */
+  const uint64_t *in;  /* device memory, n*cols words */
+  uint64_t *out;       /* device memory: n*cols words (may equal in), or
+                          blowup*n*cols for GL_OP_LDE (must not overlap in) */
+  uint32_t blowup;     /* GL_OP_LDE */
+  uint32_t reserved2;
+  uint64_t shift;      /* GL_OP_LDE coset shift */
+} gl_request;
+
+typedef struct {
+  uint64_t submitted, completed, rejected, batches, elements;
+  uint64_t max_in_use_bytes;  /* peak budgeted device memory */
+  double p50_ms, p99_ms, max_ms;  /* submit-to-completion latency of completed requests */
+} gl_server_stats;
+
+typedef struct gl_server gl_server;
+
+/* A server on the current device with `slots` concurrent batches (one CUDA
+ * stream each), at most `max_batch` requests per batch, and `budget_bytes` of
+ * device memory for the temporaries of requests in flight. */
+int gl_server_create(uint64_t budget_bytes, int slots, int max_batch, gl_server **out);
+/* Device bytes a request is budgeted for (scratch; LDE coefficients too). */
+int gl_server_request_bytes(const gl_request *req, uint64_t *bytes);
+/* Queue a request (thread-safe, non-blocking).  Rejected at once:
+ * GL_ERR_INVALID, GL_ERR_UNSUPPORTED_SIZE, or GL_ERR_BUDGET when it needs more
+ * than the whole budget. */
+int gl_server_submit(gl_server *srv, const gl_request *req, uint64_t *id);
+/* *status = the request's status: GL_ERR_BUSY while queued or running. */
+int gl_server_poll(gl_server *srv, uint64_t id, int *status);
+/* Wait up to timeout_ms for the request; GL_ERR_TIMEOUT if still pending.  On
+ * return GL_OK the request is forgotten (*status holds its result). */
+int gl_server_wait(gl_server *srv, uint64_t id, int timeout_ms, int *status);
+/* Cancel a request that has not been launched yet (GL_ERR_BUSY if it has). */
+int gl_server_cancel(gl_server *srv, uint64_t id);
+int gl_server_get_stats(gl_server *srv, gl_server_stats *out);
+/* Drain the queue and the batches in flight, then free the server. */
+int gl_server_destroy(gl_server *srv);
+
 /* ---- transform without allocation (no counterpart in the reference) ---- */
 
 /* Longest transform gl_ntt_noalloc accepts: its scratch is a fixed device

@@ -77,3 +77,14 @@ def test_lde_full_size_sampled_columns(gl, oracle, cuda):
     cols_call(gl, cuda, out, n * blowup, cols, inverse=True)
     tail = res[n:]
     assert int(cuda.count_nonzero(tail)) == 0
+
+
+def test_lde_three_pass_target(gl, oracle, cuda):
+    """n = 2^23 with blowup 8 extends to 2^26: the forward transform has three
+    passes, the coset factor and the zero padding apply to the first."""
+    n, cols, blowup = 1 << 23, 1, 8
+    x = gl.fill_uniform(n * cols, seed=0x3D)
+    d = to_dev(cuda, x)
+    out = cuda.empty(n * blowup * cols, dtype=cuda.int64, device="cuda")
+    lde_call(gl, cuda, d, out, n, cols, blowup, 7)
+    assert np.array_equal(from_dev(out), oracle.coset_lde(x, n, cols, blowup, 7))

@@ -124,3 +124,14 @@ def test_unsupported_size_raises(gl, cuda):
         gl.ntt(d)
     # Lengths 0 and 1 of intt are no-ops (ntt/src/ntt/mod.rs:105-107).
     gl.intt(cuda.zeros(1, dtype=cuda.int64, device="cuda"))
+
+
+@pytest.mark.parametrize("n", [1 << 25, 2 * 16711680])
+def test_three_pass_sizes_match_oracle(gl, oracle, cuda, n):
+    """Beyond 4096^2 the schedule has three passes (COL, COL, ROW)."""
+    x = gl.fill_uniform(n, seed=0x3A55, offset=n)
+    d = to_dev(cuda, x)
+    gl.ntt(d)
+    assert np.array_equal(from_dev(d), oracle.ntt(x))
+    gl.intt(d)
+    assert np.array_equal(from_dev(d), x)

@@ -1,0 +1,58 @@
+"""GPU: the continuous-batching server.  Each result is the same when the
+request runs alone (plain API) and when it runs in the mix with others;
+admission control, rejection, cancellation and bounded waits behave."""
+import numpy as np
+import pytest
+
+from conftest import from_dev, to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mixed_stream_matches_requests_run_alone(gl, cuda):
+    from goldilocks_gb300 import server as S
+    reqs = S.make_requests(60, seed=7, log_min=6, log_max=16, max_cols=8)
+    pool = to_dev(cuda, gl.fill_uniform(max(n * c for _, n, c, _ in reqs), seed=11))
+    arrivals = S.poisson_arrivals(len(reqs), rate_per_s=2000.0, seed=7)
+    _, stats, _, mixed = S.serve_stream(reqs, arrivals, pool, budget_bytes=1 << 26, slots=3,
+                                        max_batch=16)
+    _, _, _, alone = S.serial_baseline(reqs, pool)
+    for r, a, b in zip(reqs, mixed, alone):
+        assert np.array_equal(from_dev(a), from_dev(b)), r
+    assert stats["completed"] == len(reqs) and stats["batches"] >= 1
+    assert stats["max_in_use_bytes"] <= 1 << 26
+
+
+def test_lde_request_matches_oracle(gl, oracle, cuda):
+    from goldilocks_gb300 import server as S
+    n, cols = 1024, 3
+    x = gl.fill_uniform(n * cols, seed=3)
+    inp = to_dev(cuda, x)
+    out = cuda.empty(4 * n * cols, dtype=cuda.int64, device="cuda")
+    with S.Server(budget_bytes=1 << 30, slots=2, max_batch=4) as srv:
+        rid = srv.submit(S.GL_OP_LDE, n, cols, inp, out, blowup=4, shift=7)
+        assert srv.wait(rid) == gl._lib.GL_OK
+    assert np.array_equal(from_dev(out), oracle.coset_lde(x, n, cols, 4, 7))
+
+
+def test_rejections_cancellation_and_bounded_wait(gl, cuda):
+    from goldilocks_gb300 import server as S
+    L = gl._lib
+    buf = cuda.zeros(1 << 16, dtype=cuda.int64, device="cuda")
+    with S.Server(budget_bytes=1 << 20, slots=1, max_batch=1) as srv:
+        with pytest.raises(gl.GoldilocksError) as e:   # needs more than the whole budget
+            srv.submit(S.GL_OP_NTT, 1 << 16, 1, buf, buf)
+        assert e.value.status == L.GL_ERR_BUDGET
+        with pytest.raises(gl.GoldilocksError) as e:   # not a divisor of p - 1
+            srv.submit(S.GL_OP_NTT, 7, 1, buf, buf)
+        assert e.value.status == L.GL_ERR_UNSUPPORTED_SIZE
+        # A queue behind a busy slot: the later request can be cancelled.
+        ids = [srv.submit(S.GL_OP_NTT, 4096, 8, buf, buf) for _ in range(6)]
+        cancelled = [rid for rid in ids[1:] if srv.cancel(rid) == L.GL_OK]
+        for rid in ids:
+            st = srv.wait(rid, timeout_ms=60000)
+            assert st == (L.GL_ERR_CANCELLED if rid in cancelled else L.GL_OK)
+        with pytest.raises(gl.GoldilocksError) as e:
+            srv.wait(123456789)
+        assert e.value.status == L.GL_ERR_NOT_FOUND
+        assert srv.stats()["rejected"] == 2
