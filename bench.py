@@ -166,6 +166,59 @@ def run_reference(args):
     return 0
 
 
+def bench_batched(gl, torch, reps=3):
+    """Config 3: 1024 polynomials, log2 n ~ U[12, 18] (seeded), odd index
+    inverse, one batch per step; elements/s per execution mode."""
+    import numpy as np
+    from goldilocks_gb300 import batch as B
+    rng = np.random.default_rng(0xBA7C)
+    sizes = [1 << int(k) for k in rng.integers(12, 19, 1024)]
+    pool = torch.from_numpy(gl.fill_uniform(sum(sizes), seed=0xBA7C).view(np.int64)).cuda()
+    items, off = [], 0
+    for i, n in enumerate(sizes):
+        items.append((pool[off:off + n], i % 2))
+        off += n
+    out = {"polys": len(sizes), "elements": int(sum(sizes))}
+    stream = torch.cuda.current_stream()
+    for name, mode in (("per_call", B.PER_CALL), ("buckets", B.BUCKETS), ("persistent", B.PERSISTENT)):
+        B.run(items, mode=mode)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            B.run(items, mode=mode)
+        b.record(stream)
+        b.synchronize()
+        out[name + "_elem_s"] = out["elements"] * reps / (a.elapsed_time(b) * 1e-3)
+    out["persistent_vs_per_call"] = out["persistent_elem_s"] / out["per_call_elem_s"]
+    return out
+
+
+def bench_serving(gl, torch, count=300, log_max=20):
+    """Config 5 (scaled): Poisson stream of NTT/iNTT/LDE (40/30/30) requests,
+    log2 n ~ U[10, log_max], 1..64 columns, 64 GB admission budget; served
+    (continuous batching) vs serial plain launches on the same GPU."""
+    from goldilocks_gb300 import server as S
+    import numpy as np
+    reqs = S.make_requests(count, seed=0x5E77, log_min=10, log_max=log_max, max_cols=64)
+    pool = torch.from_numpy(gl.fill_uniform(max(n * c for _, n, c, _ in reqs), seed=5).view(np.int64)).cuda()
+    ser_rate, ser_lat, ser_wall, outs = S.serial_baseline(reqs, pool)
+    del outs
+    res = {"requests": count, "log2_n": [10, log_max], "mix": "40/30/30 ntt/intt/lde, blowup 4",
+           "serial_elem_s": ser_rate, "serial_p50_ms": ser_lat["p50_ms"], "serial_p99_ms": ser_lat["p99_ms"],
+           "sweep": []}
+    offered = count / ser_wall  # requests/s the serial path sustains
+    for load in (0.5, 2.0):
+        arrivals = S.poisson_arrivals(count, rate_per_s=offered * load, seed=0x5E77)
+        rate, stats, wall, outs = S.serve_stream(reqs, arrivals, pool, budget_bytes=64 << 30, slots=4,
+                                                 max_batch=64)
+        del outs
+        res["sweep"].append({"offered_req_s": offered * load, "served_elem_s": rate,
+                             "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"],
+                             "batches": stats["batches"]})
+    return res
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -297,6 +350,15 @@ def run_ours(args):
                               "frac": alg_bytes / (step_ms * 1e-3) / 1e9 / peak},
             "e2e": e2e, "gpu_launches": launches, "clocks": clk,
             "kernels": prof}
+    if world == 1 and not args.no_extras:
+        try:
+            line["batched"] = bench_batched(gl, torch)
+        except Exception as e:  # reported, not fatal to the headline line
+            line["batched"] = {"error": str(e)}
+        try:
+            line["serving"] = bench_serving(gl, torch)
+        except Exception as e:
+            line["serving"] = {"error": str(e)}
     if world == 1 and not args.no_cpu_baseline:
         threads = min(2 * len(SIZES), os.cpu_count() or 1)
         el, s = cpu_oracle_step(threads)
@@ -316,6 +378,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched and serving figures")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -38,18 +38,20 @@ struct gl_work {
 };
 
 constexpr int kNT = 1024;
-constexpr int kLanes = 4;
 
-// Shapes the persistent kernel is compiled for: (r1, r2, r3), forward then
-// inverse.  Index = 2 * position + inverse.
-#define GL_BATCH_SHAPES(X) \
-  X(8, 8, 1) X(16, 8, 1) X(16, 16, 1) X(8, 8, 8) X(16, 8, 8) X(16, 16, 8) X(16, 16, 16) X(16, 15, 17)
+// Shapes the persistent kernel is compiled for: (r1, r2, r3, lanes per work
+// item), forward then inverse; index = 2 * position + inverse.  The lane
+// count makes every shape occupy the 1024 threads of the CTA (lanes x the
+// largest number of radix groups per lane = 1024).
+#define GL_BATCH_SHAPES(X)                                                               \
+  X(8, 8, 1, 128) X(16, 8, 1, 64) X(16, 16, 1, 64) X(8, 8, 8, 16) X(16, 8, 8, 8) X(16, 16, 8, 4) \
+  X(16, 16, 16, 4) X(16, 15, 17, 4)
 
 struct shape_desc {
-  int r1, r2, r3;
+  int r1, r2, r3, lanes;
   size_t smem;
 };
-#define GL_SHAPE_DESC(A, B, C) {A, B, C, gl_p3_smem_bytes<A, B, C, kLanes>()},
+#define GL_SHAPE_DESC(A, B, C, LN) {A, B, C, LN, gl_p3_smem_bytes<A, B, C, LN>()},
 const shape_desc kShapes[] = {GL_BATCH_SHAPES(GL_SHAPE_DESC)};
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
@@ -80,9 +82,9 @@ __device__ __forceinline__ uint64_t globaltimer() {
 
 __device__ void dispatch(uint32_t shape, const gl_pass_args &a, int64_t bx, uint64_t *sm) {
   int i = 0;
-#define GL_DISPATCH(A, B, C)                                                 \
-  if (shape == (uint32_t)(2 * i)) { gl_block3<A, B, C, kLanes, kNT, false>(a, bx, 0, 0, sm); return; } \
-  if (shape == (uint32_t)(2 * i + 1)) { gl_block3<A, B, C, kLanes, kNT, true>(a, bx, 0, 0, sm); return; } \
+#define GL_DISPATCH(A, B, C, LN)                                                                   \
+  if (shape == (uint32_t)(2 * i)) { gl_block3<A, B, C, LN, kNT, false>(a, bx, 0, 0, sm); return; }  \
+  if (shape == (uint32_t)(2 * i + 1)) { gl_block3<A, B, C, LN, kNT, true>(a, bx, 0, 0, sm); return; } \
   i++;
   GL_BATCH_SHAPES(GL_DISPATCH)
 #undef GL_DISPATCH
@@ -244,10 +246,12 @@ int enqueue_persistent(const gl_poly *polys, uint64_t count, const std::vector<p
   std::vector<gl_work> items;
   std::deque<std::pair<uint64_t, size_t>> pending;  // (poly, queue position after its col tiles)
   const size_t lag = 2 * (size_t)sms;
+  auto lanes_of = [](int shape) { return (uint64_t)kShapes[shape / 2].lanes; };
+  auto tiles = [](uint64_t lanes, uint64_t per) { return (uint32_t)((lanes + per - 1) / per); };
   auto push_rows = [&](uint64_t i) {
     const gl_plan *pl = pp[i].pl;
-    const uint32_t col_tiles = (uint32_t)(pl->n2 / kLanes);
-    for (uint32_t t = 0; t < pl->n1 / kLanes; t++)
+    const uint32_t col_tiles = tiles(pl->n2, lanes_of(shape_col[i]));
+    for (uint32_t t = 0; t < tiles(pl->n1, lanes_of(shape_row[i])); t++)
       items.push_back({(uint32_t)shape_row[i], 2, (uint32_t)i, t, (uint32_t)(2 * i + 1), col_tiles});
   };
   for (uint64_t i = 0; i < count; i++) {
@@ -256,7 +260,7 @@ int enqueue_persistent(const gl_poly *polys, uint64_t count, const std::vector<p
     if (pl->kind == 1) {
       items.push_back({(uint32_t)shape_col[i], 0, (uint32_t)i, 0, (uint32_t)(2 * i), 0});
     } else if (pl->kind == 2) {
-      for (uint32_t t = 0; t < pl->n2 / kLanes; t++)
+      for (uint32_t t = 0; t < tiles(pl->n2, lanes_of(shape_col[i])); t++)
         items.push_back({(uint32_t)shape_col[i], 1, (uint32_t)i, t, (uint32_t)(2 * i), 0});
       pending.push_back({i, items.size()});
     }
@@ -398,12 +402,12 @@ int run_buckets(const gl_poly *polys, uint64_t count, const std::vector<poly_pla
         col.flags |= GL_PF_PTR_TABLE;
         col.in_ptrs = (const uint64_t *const *)(dt + j);
         col.out_ptrs = (uint64_t *const *)(dt + base_sc + j);
-        gl_launch(pl->k[0][d], 1, col, dim3((unsigned)(pl->n2 / kLanes), (unsigned)(j1 - j)),
+        gl_launch(pl->k[0][d], 1, col, dim3((unsigned)(pl->n2 / GL_PASS_LANES), (unsigned)(j1 - j)),
                   pl->size * (j1 - j), cap);
         row.flags |= GL_PF_PTR_TABLE;
         row.in_ptrs = (const uint64_t *const *)(dt + base_sc + j);
         row.out_ptrs = (uint64_t *const *)(dt + j);
-        gl_launch(pl->k[1][d], 2, row, dim3((unsigned)(pl->n1 / kLanes), (unsigned)(j1 - j)),
+        gl_launch(pl->k[1][d], 2, row, dim3((unsigned)(pl->n1 / GL_PASS_LANES), (unsigned)(j1 - j)),
                   pl->size * (j1 - j), cap);
       }
       j = j1;

@@ -41,7 +41,7 @@ def test_rejections_cancellation_and_bounded_wait(gl, cuda):
     buf = cuda.zeros(1 << 16, dtype=cuda.int64, device="cuda")
     with S.Server(budget_bytes=1 << 20, slots=1, max_batch=1) as srv:
         with pytest.raises(gl.GoldilocksError) as e:   # needs more than the whole budget
-            srv.submit(S.GL_OP_NTT, 1 << 16, 1, buf, buf)
+            srv.submit(S.GL_OP_NTT, 1 << 18, 1, buf, buf)
         assert e.value.status == L.GL_ERR_BUDGET
         with pytest.raises(gl.GoldilocksError) as e:   # not a divisor of p - 1
             srv.submit(S.GL_OP_NTT, 7, 1, buf, buf)
