@@ -15,8 +15,12 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
+# GOLDILOCKS_BUILD_DIR and GOLDILOCKS_NVCC_FLAGS select another build
+# directory and extra nvcc flags (e.g. -D switches of alternative code paths),
+# so that variants can be built side by side and compared.
+BUILD = os.environ.get("GOLDILOCKS_BUILD_DIR") or os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgoldilocks_gpu.so")
+EXTRA_FLAGS = os.environ.get("GOLDILOCKS_NVCC_FLAGS", "").split()
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -37,7 +41,7 @@ def _headers_digest():
                     + glob.glob(os.path.join(INCLUDE, "*.h"))):
         with open(p, "rb") as f:
             h.update(p.encode() + f.read())
-    h.update(" ".join(ARCH + NVCC_FLAGS).encode())
+    h.update(" ".join(ARCH + NVCC_FLAGS + EXTRA_FLAGS).encode())
     return h.hexdigest()
 
 
@@ -45,7 +49,7 @@ def _compile(src, obj, stamp, digest, verbose):
     key = digest + hashlib.sha256(open(src, "rb").read()).hexdigest()
     if os.path.exists(obj) and os.path.exists(stamp) and open(stamp).read() == key:
         return obj, False
-    cmd = [nvcc()] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + ARCH + NVCC_FLAGS + EXTRA_FLAGS + ["-c", src, "-o", obj]
     if verbose:
         sys.stderr.write(" ".join(cmd) + "\n")
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -126,10 +126,39 @@ GL_HD uint64_t gl_reduce159(uint64_t low, uint64_t mid, uint64_t high) {
 }
 
 #ifdef GL_DEV_PTX
-// l + h0*2^64 - h1*2^96 ... as 32-bit words: value = (l1:l0) - h1 + h0*EPS,
-// with h0, h1 < 2^32; canonical result.
+// A 32-bit constant the compiler cannot see through, so that multiplications
+// by it stay integer multiply-adds (FMA pipe) instead of becoming shifts (ALU).
+__device__ __forceinline__ uint32_t gl_opaque(uint32_t c) {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %1;" : "=r"(r) : "r"(c));
+  return r;
+}
+
+// value = (l1:l0) + h0*2^64 + h1*2^96 = (l1:l0) - h1 + h0*EPS (mod p), with
+// h0, h1 < 2^32; canonical result.
 __device__ __forceinline__ uint64_t gl_reduce_words(uint32_t l0, uint32_t l1, uint32_t h0,
                                                     uint32_t h1) {
+#ifdef GL_FIELD_V2
+  // h0*EPS as one 32x32->64 multiply (integer FMA pipe) instead of two ALU ops.
+  const uint64_t u = (uint64_t)h0 * gl_opaque(0xffffffffu);
+  uint32_t u0, u1;
+  gl_unpack(u, u0, u1);
+  uint32_t t0, t1, m, c;
+  asm("sub.cc.u32 %0, %4, %7;\n\t"       // t = l - h1
+      "subc.cc.u32 %1, %5, 0;\n\t"
+      "subc.u32 %2, 0, 0;\n\t"
+      "sub.cc.u32 %0, %0, %2;\n\t"       // borrow: + p
+      "subc.u32 %1, %1, 0;\n\t"
+      "add.cc.u32 %0, %0, %8;\n\t"       // t += u
+      "addc.cc.u32 %1, %1, %9;\n\t"
+      "addc.u32 %3, 0, 0;\n\t"
+      "sub.u32 %2, 0, %3;\n\t"           // carry: + EPS
+      "add.cc.u32 %0, %0, %2;\n\t"
+      "addc.u32 %1, %1, 0;"
+      : "=&r"(t0), "=&r"(t1), "=&r"(m), "=&r"(c)
+      : "r"(l0), "r"(l1), "r"(h0), "r"(h1), "r"(u0), "r"(u1));
+  return gl_canon32(t0, t1);
+#else
   uint32_t t0, t1, m, u0, u1, c;
   asm("sub.cc.u32 %0, %6, %9;\n\t"       // t = l - h1
       "subc.cc.u32 %1, %7, 0;\n\t"
@@ -147,6 +176,7 @@ __device__ __forceinline__ uint64_t gl_reduce_words(uint32_t l0, uint32_t l1, ui
       : "=&r"(t0), "=&r"(t1), "=&r"(m), "=&r"(u0), "=&r"(u1), "=&r"(c)
       : "r"(l0), "r"(l1), "r"(h0), "r"(h1));
   return gl_canon32(t0, t1);
+#endif
 }
 #endif
 
@@ -199,6 +229,25 @@ GL_HD uint64_t gl_shl(uint64_t x) {
     uint32_t x0, x1;
     gl_unpack(x, x0, x1);
     uint32_t w0, w1, w2, w3;
+#ifdef GL_FIELD_V2
+    if constexpr (K < 32 || (K > 32 && K < 64) || (K > 64 && K < 96)) {
+      // x * 2^s (s = K mod 32) as 32x32->64 multiply-adds on the FMA pipe.
+      constexpr int sh = K % 32;
+      const uint32_t c = gl_opaque(1u << sh);
+      const uint64_t p0 = (uint64_t)x0 * c;
+      const uint64_t p1 = (uint64_t)x1 * c + (p0 >> 32);
+      const uint32_t a0 = (uint32_t)p0, a1 = (uint32_t)p1, a2 = (uint32_t)(p1 >> 32);
+      if constexpr (K < 32) {
+        w0 = a0; w1 = a1; w2 = a2; w3 = 0;
+      } else if constexpr (K < 64) {
+        w0 = 0; w1 = a0; w2 = a1; w3 = a2;
+      } else {
+        // 64 < K < 96: x*2^K = a0*2^64 + a1*2^96 + a2*2^128, 2^128 = -2^32.
+        return gl_reduce_words(1u, 0xffffffffu - a2, a0, a1);
+      }
+      return gl_reduce_words(w0, w1, w2, w3);
+    }
+#endif
     if constexpr (K < 32) {
       w0 = x0 << K;
       w1 = __funnelshift_l(x0, x1, K);
