@@ -178,7 +178,7 @@ def dft_int(x, inv=False):
     return [sum(x[j] * pow(w, j * k % n, P) for j in range(n)) % P for k in range(n)]
 
 
-SIZES = [2, 3, 4, 5, 8, 15, 16, 17, 32, 60, 64, 68]
+SIZES = [2, 3, 4, 5, 6, 8, 10, 12, 15, 16, 17, 32, 60, 64, 68]
 
 
 def emit(sizes=SIZES):

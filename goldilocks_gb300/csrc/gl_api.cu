@@ -134,6 +134,42 @@ static const gl_kernel_entry *find_in(const gl_kernel_entry *e, size_t cnt, uint
   return nullptr;
 }
 
+// Radices of the run-time kernel: m = r1*r2*r3 (r2, r3 may be 1) from the
+// codelet sizes <= 17, fewest rounds first, larger radices first.
+static bool generic_radices(uint64_t m, int r[3]) {
+  static const int R[] = {17, 16, 15, 12, 10, 8, 6, 5, 4, 3, 2};
+  if (m < 2 || m > 4096) return false;
+  for (int a : R)
+    if ((uint64_t)a == m) { r[0] = a; r[1] = 1; r[2] = 1; return true; }
+  for (int a : R)
+    for (int b : R)
+      if ((uint64_t)a * b == m) { r[0] = a; r[1] = b; r[2] = 1; return true; }
+  for (int a : R)
+    for (int b : R)
+      for (int c : R)
+        if ((uint64_t)a * b * c == m) { r[0] = a; r[1] = b; r[2] = c; return true; }
+  return false;
+}
+
+static const gl_kernel_entry *generic_entry(uint64_t m, bool inv) {
+  static std::mutex mu;
+  static std::map<std::pair<uint64_t, bool>, gl_kernel_entry> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_pair(m, inv);
+  auto it = cache.find(key);
+  if (it != cache.end()) return &it->second;
+  int r[3];
+  if (!generic_radices(m, r)) return nullptr;
+  gl_kernel_entry e{};
+  e.m = (int)m; e.r1 = r[0]; e.r2 = r[1]; e.r3 = r[2];
+  e.lanes = GL_GEN_LANES; e.inv = inv;
+  e.smem = r[1] == 1 ? 0 : (size_t)GL_GEN_LANES * gl_gen_ls((int)m) * sizeof(uint64_t);
+  e.threads = GL_GEN_NT;
+  e.launch = inv ? gl_launch_generic_inv : gl_launch_generic_fwd;
+  e.generic = true;
+  return &cache.emplace(key, e).first->second;
+}
+
 const gl_kernel_entry *gl_find_kernel(uint64_t m, bool full, bool inv) {
   size_t cnt = 0;
   if (!full && use_wide_kernels()) {
@@ -142,7 +178,8 @@ const gl_kernel_entry *gl_find_kernel(uint64_t m, bool full, bool inv) {
   }
   const gl_kernel_entry *e = full ? (inv ? gl_kernels_full_inv(&cnt) : gl_kernels_full_fwd(&cnt))
                                   : (inv ? gl_kernels_pass_inv(&cnt) : gl_kernels_pass_fwd(&cnt));
-  return find_in(e, cnt, m);
+  if (const gl_kernel_entry *k = find_in(e, cnt, m)) return k;
+  return generic_entry(m, inv);  // every other size up to 4096 with radices <= 17
 }
 
 static std::string kernel_shape(const gl_kernel_entry *k) {
@@ -409,8 +446,10 @@ static std::string kernel_label(const gl_kernel_entry *k, int role) {
 }
 
 // Launch `k` with optional event bracketing.  role: 0 full, 1 col, 2 row.
-void gl_launch(const gl_kernel_entry *k, int role, const gl_pass_args &a, dim3 grid,
+void gl_launch(const gl_kernel_entry *k, int role, const gl_pass_args &a0, dim3 grid,
                    uint64_t elements, cudaStream_t stream) {
+  gl_pass_args a = a0;
+  if (k->generic) { a.gen_r[0] = k->r1; a.gen_r[1] = k->r2; a.gen_r[2] = k->r3; }
   bool on;
   { std::lock_guard<std::mutex> lk(g_prof_mu); on = g_prof_on; }
   if (!on) { k->launch(a, grid, stream); return; }

@@ -23,6 +23,7 @@ struct gl_kernel_entry {
   size_t smem;        // dynamic shared memory bytes
   int threads;
   gl_launch_fn launch;
+  bool generic = false;  // gl_generic_kernel: radices passed at run time
 };
 
 // Kernel sets compiled in separate translation units (parallel build).
@@ -36,6 +37,11 @@ const gl_kernel_entry *gl_kernels_pass_inv(size_t *count);
 // autotuner may choose).
 const gl_kernel_entry *gl_kernels_wide_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_wide_inv(size_t *count);
+
+// Run-time-radix kernels (gl_kern_generic.cu).
+void gl_launch_generic_fwd(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
+void gl_launch_generic_inv(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
+#include "gl_generic.cuh"
 
 // Launch-time check: the kernel entry for (m, full, inv), or nullptr.
 const gl_kernel_entry *gl_find_kernel(uint64_t m, bool full, bool inv);

@@ -1,0 +1,6 @@
+// Run-time-radix pass kernel, forward direction.
+#include "gl_kern_generic_impl.cuh"
+
+void gl_launch_generic_fwd(const gl_pass_args &args, dim3 grid, cudaStream_t stream) {
+  gl_launch_generic<false>(args, grid, stream);
+}

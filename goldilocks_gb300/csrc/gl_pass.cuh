@@ -53,6 +53,7 @@ struct gl_pass_args {
   int64_t tw_ld;
   const uint64_t *const *in_ptrs;  // GL_PF_PTR_TABLE: base pointer of batch item by
   uint64_t *const *out_ptrs;
+  int32_t gen_r[3];                 // run-time radices of gl_generic_kernel
 };
 
 // Pass twiddle omega_n^(col*k): from the full table when present, else from

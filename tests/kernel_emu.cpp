@@ -30,6 +30,7 @@ static std::barrier<> *g_bar = nullptr;
 uint64_t sm[1 << 16];  // the CTA's dynamic shared memory
 
 #include "gl_pass3.cuh"
+#include "gl_generic.cuh"
 
 template <int R1, int R2, int R3, int LANES, int NT, bool INV>
 static void run_grid(const gl_pass_args &a, unsigned gx, unsigned gy, unsigned gz) {
@@ -50,14 +51,48 @@ static void run_grid(const gl_pass_args &a, unsigned gx, unsigned gy, unsigned g
       }
 }
 
+template <bool INV>
+static void run_generic(const gl_pass_args &a, unsigned gx) {
+  for (unsigned x = 0; x < gx; x++) {
+    blockIdx.x = x; blockIdx.y = 0; blockIdx.z = 0;
+    memset(sm, 0xA5, sizeof(sm));
+    std::barrier<> bar(GL_GEN_NT);
+    g_bar = &bar;
+    std::vector<std::thread> th;
+    for (int t = 0; t < GL_GEN_NT; t++)
+      th.emplace_back([&a, t] {
+        threadIdx.x = t;
+        gl_generic_kernel<INV>(a);
+      });
+    for (auto &t : th) t.join();
+  }
+}
+
+#define EMU_ARGS                                                                              \
+  int r1, int r2, int r3, int inv, const uint64_t *in, uint64_t *out, int64_t in_ls,            \
+      int64_t in_is, int64_t out_ls, int64_t out_is, uint32_t lanes, uint32_t flags,            \
+      const uint64_t *tw_m, const uint64_t *tw_r2, const uint64_t *tw_lo, const uint64_t *tw_hi, \
+      uint32_t tw_lane_div, uint32_t in_limit, const uint64_t *itw_lo, const uint64_t *itw_hi,  \
+      uint64_t itw_jmul
+
 extern "C" {
+// Emulated launch of the run-time-radix kernel with radices r1*r2*r3.
+int emu_generic(EMU_ARGS) {
+  gl_pass_args a{};
+  a.in = in; a.out = out;
+  a.in_ls = in_ls; a.in_is = in_is; a.out_ls = out_ls; a.out_is = out_is;
+  a.lanes = lanes; a.flags = flags; a.tw_m = tw_m; a.tw_r2 = tw_r2; a.tw_lo = tw_lo; a.tw_hi = tw_hi;
+  a.tw_lane_div = tw_lane_div; a.in_limit = in_limit;
+  a.itw_lo = itw_lo; a.itw_hi = itw_hi; a.itw_jmul = itw_jmul;
+  a.gen_r[0] = r1; a.gen_r[1] = r2; a.gen_r[2] = r3;
+  const unsigned gx = (lanes + GL_GEN_LANES - 1) / GL_GEN_LANES;
+  if (inv) run_generic<true>(a, gx);
+  else run_generic<false>(a, gx);
+  return 0;
+}
+
 // Emulated launch of one compiled shape; returns -1 for an unknown shape.
-int emu_pass3(int r1, int r2, int r3, int inv, const uint64_t *in, uint64_t *out, int64_t in_ls,
-              int64_t in_is, int64_t out_ls, int64_t out_is, uint32_t lanes, uint32_t flags,
-              const uint64_t *tw_m, const uint64_t *tw_r2, const uint64_t *tw_lo,
-              const uint64_t *tw_hi,
-              uint32_t tw_lane_div, uint32_t in_limit, const uint64_t *itw_lo,
-              const uint64_t *itw_hi, uint64_t itw_jmul) {
+int emu_pass3(EMU_ARGS) {
   gl_pass_args a{};
   a.in = in; a.out = out;
   a.in_ls = in_ls; a.in_is = in_is; a.out_ls = out_ls; a.out_is = out_is;

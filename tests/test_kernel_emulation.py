@@ -25,8 +25,9 @@ def emu(tmp_path_factory):
                     os.path.join(HERE, "kernel_emu.cpp"), "-o", str(so)], check=True)
     lib = ctypes.CDLL(str(so))
     vp, i64, u32, u64 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint64
-    lib.emu_pass3.argtypes = [ctypes.c_int] * 4 + [vp, vp, i64, i64, i64, i64, u32, u32,
-                                                   vp, vp, vp, vp, u32, u32, vp, vp, u64]
+    for f in (lib.emu_pass3, lib.emu_generic):
+        f.argtypes = [ctypes.c_int] * 4 + [vp, vp, i64, i64, i64, i64, u32, u32,
+                                           vp, vp, vp, vp, u32, u32, vp, vp, u64]
     return lib
 
 
@@ -45,17 +46,25 @@ def table(w, count, scale=1):
 
 def call(emu, shape, inv, x, out, in_ls, in_is, out_ls, out_is, lanes, flags, tw_m, tw_r2,
          tw_lo=None, tw_hi=None, lane_div=1, in_limit=NOLIM, itw_lo=None, itw_hi=None, jmul=0):
+    """`shape` = (r1, r2, r3) of a compiled kernel, or ("gen", r1, r2, r3) for
+    the run-time-radix kernel."""
     ptr = lambda a: None if a is None else a.ctypes.data
-    rc = emu.emu_pass3(*shape, int(inv), ptr(x), ptr(out), in_ls, in_is, out_ls, out_is, lanes, flags,
+    fn = emu.emu_pass3
+    if shape[0] == "gen":
+        fn, shape = emu.emu_generic, shape[1:]
+    rc = fn(*shape, int(inv), ptr(x), ptr(out), in_ls, in_is, out_ls, out_is, lanes, flags,
                        ptr(tw_m), ptr(tw_r2), ptr(tw_lo), ptr(tw_hi), lane_div, in_limit,
                        ptr(itw_lo), ptr(itw_hi), jmul)
     assert rc == 0
 
 
-@pytest.mark.parametrize("shape", [(8, 8, 1), (16, 16, 1), (8, 8, 8), (16, 8, 8)])
+@pytest.mark.parametrize("shape", [(8, 8, 1), (16, 16, 1), (8, 8, 8), (16, 8, 8),
+                                   ("gen", 3, 1, 1), ("gen", 17, 1, 1), ("gen", 17, 15, 1),
+                                   ("gen", 12, 10, 1), ("gen", 5, 6, 17), ("gen", 17, 16, 15)])
 @pytest.mark.parametrize("inv", [False, True])
 def test_whole_transforms_on_columns(emu, oracle, shape, inv):
-    m = shape[0] * shape[1] * shape[2]
+    r = shape[1:] if shape[0] == "gen" else shape
+    m = r[0] * r[1] * r[2]
     cols = 5
     x = rand_field(m * cols, seed=m + inv)
     out = np.zeros_like(x)
@@ -95,6 +104,16 @@ def test_four_step(emu, oracle, inv):
     n1, n2 = 64, 512
     x = rand_field(n1 * n2, seed=7 + inv)
     got = four_step(emu, n1, n2, (8, 8, 1), (8, 8, 8), x, inv)
+    assert np.array_equal(got, (oracle.intt if inv else oracle.ntt)(x))
+
+
+@pytest.mark.parametrize("inv", [False, True])
+def test_four_step_run_time_radices(emu, oracle, inv):
+    """Factors 3, 5 and 17 in the column pass: 255 x 64 with both passes run by
+    the run-time-radix kernel."""
+    n1, n2 = 255, 64
+    x = rand_field(n1 * n2, seed=17 + inv)
+    got = four_step(emu, n1, n2, ("gen", 17, 15, 1), ("gen", 16, 4, 1), x, inv)
     assert np.array_equal(got, (oracle.intt if inv else oracle.ntt)(x))
 
 
