@@ -1,8 +1,8 @@
 """GB300-native (sm_103a) Goldilocks NTT: a drop-in for the transform path of
 recmo/goldilocks' `goldilocks-ntt` crate behind a C ABI (include/goldilocks_gpu.h).
 """
-from .ntt import (MODULUS, GoldilocksError, Plan, clear_cache, divisors, fill_uniform,
+from .ntt import (MODULUS, GoldilocksError, Plan, clear_cache, convolve, divisors, fill_uniform,
                   intt, is_divisor, next, ntt, split, strategy)
 
-__all__ = ["MODULUS", "GoldilocksError", "Plan", "clear_cache", "divisors", "fill_uniform",
+__all__ = ["MODULUS", "GoldilocksError", "Plan", "clear_cache", "convolve", "divisors", "fill_uniform",
            "intt", "is_divisor", "next", "ntt", "split", "strategy"]

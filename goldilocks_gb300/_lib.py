@@ -35,6 +35,7 @@ SIGNATURES = [
     ("gl_fill_uniform", None, [_vp, _u64, _u64, _u64]),
     ("gl_ntt_columns", _int, [_vp, _u64, _u64, _int, _int, _vp]),
     ("gl_coset_lde", _int, [_vp, _vp, _u64, _u64, _u32, _u64, _int, _vp]),
+    ("gl_convolve", _int, [_vp, _vp, _u64, _u64, _u64, _int, _int, _vp]),
     ("gl_batch_execute", _int, [_vp, _u64, _int, _vp]),
     ("gl_batch_autotune", _int, [_vp, _u64, _int, _vp, _vp]),
     ("gl_server_create", _int, [_u64, _int, _int, ctypes.POINTER(_vp)]),
@@ -60,6 +61,8 @@ GL_BATCH_AUTO, GL_BATCH_PERSISTENT, GL_BATCH_BUCKETS, GL_BATCH_PER_CALL = 0, 1, 
 
 
 GL_OP_NTT, GL_OP_INTT, GL_OP_LDE = 0, 1, 2
+
+GL_REPR_CANONICAL, GL_REPR_MONTGOMERY = 0, 1
 
 
 class Request(ctypes.Structure):

@@ -498,24 +498,20 @@ extern "C" int gl_profile_read(gl_profile_entry *out, int cap) {
 
 static const uint64_t kMaxGridYZ = 65535;
 
-// Optional load-side transformation (the LDE's zero padding and coset shift).
-struct gl_load_opts {
-  uint32_t in_limit = 0xffffffffu;   // rows >= in_limit read as zero
-  const uint64_t *itw_lo = nullptr;  // g^e, e < 4096
-  const uint64_t *itw_hi = nullptr;  // g^(4096 e)
-};
-
 // Queue the transform of a strided batch on `stream`.  Element j of column c
 // of batch item b is at base[b*bs + j*C + c] (C = 1, bs = n: contiguous
 // transforms; C = cols, B = 1: the columns of a row-major matrix).  `src` and
 // `dst` may be equal.  Two-pass plans use `scratch` (>= n*C*B words).
-static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64_t C,
-                             uint64_t B, uint64_t bs, bool inv, uint64_t *scratch,
-                             cudaStream_t stream, const gl_load_opts *lo = nullptr) {
+int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64_t C, uint64_t B,
+                         uint64_t bs, bool inv, uint64_t *scratch, cudaStream_t stream,
+                         const gl_load_opts *lo, const gl_store_mul *om) {
   if (B == 0 || C == 0) return GL_OK;
   const uint64_t n = pl->size;
   gl_load_opts none;
   if (!lo) lo = &none;
+  if (om && (C != 1 || pl->kind == 0)) return GL_ERR_INVALID;  // contiguous transforms only
+  const uint32_t mul_flags = om ? (GL_PF_OUT_MUL | (om->mont ? GL_PF_OUT_MUL_MONT : 0u)) : 0u;
+  const int64_t mul_item = om && !om->shared ? (int64_t)n : 0;  // factor stride per item
   if (pl->kind == 0) {
     if (src != dst) {
       for (uint64_t b = 0; b < B; b++) {
@@ -552,10 +548,12 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
       // Lanes are batch items (stride bs).
       a.in_ls = a.out_ls = (int64_t)bs; a.in_is = a.out_is = 1;
       if (coset) { a.itw_jmul = 1; a.tw_lane_div = 0xffffffffu; }
+      if (om) { a.flags |= mul_flags; a.mul_ls = mul_item; }  // lane = batch item
       const uint64_t per = (uint64_t)k->lanes * 0x7fffffffull;
       for (uint64_t off = 0; off < B; off += per) {
         const uint64_t c = std::min(per, B - off);
         a.in = src + off * bs; a.out = dst + off * bs;
+        if (om) a.mul = om->factors + off * mul_item;
         a.lanes = (uint32_t)c;
         gl_launch(k, 0, a, dim3((unsigned)((c + k->lanes - 1) / k->lanes)), c * n, stream);
       }
@@ -623,6 +621,11 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
         c.out_ls = (int64_t)n1; c.out_is = (int64_t)(n1 * n2);
         c.in_bs = (int64_t)n23; c.out_bs = 1;                     // grid.y: k1
         c.lanes = (uint32_t)n2;
+        if (om) {  // output offset k1 + n1 k2 + n1 n2 k3 is the frequency index
+          c.flags |= mul_flags;
+          c.mul = om->factors + b * mul_item;
+          c.mul_ls = c.out_ls; c.mul_bs = c.out_bs;
+        }
         gl_launch(kcr, 2, c, dim3((unsigned)(n2 / GL_PASS_LANES), (unsigned)n1), n, stream);
       } else {
         c.in_ls = 1; c.in_is = (int64_t)C;                        // lanes: columns
@@ -674,6 +677,11 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
       b.in_ls = (int64_t)n2; b.in_is = 1; b.out_ls = 1; b.out_is = (int64_t)n1;
       b.in_bs = (int64_t)n; b.out_bs = (int64_t)bs;
       b.lanes = (uint32_t)n1;
+      if (om) {  // output offset k1 + n1 k2 is the frequency index
+        b.flags |= mul_flags;
+        b.mul = om->factors + off * mul_item;
+        b.mul_ls = 1; b.mul_bs = mul_item;
+      }
       gl_launch(kr, 2, b, dim3((unsigned)(n1 / GL_PASS_LANES), (unsigned)cb), cb * n, stream);
     } else {
       b.in = scratch + off * n * C; b.out = dst + off * bs;
@@ -691,7 +699,7 @@ static int enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, ui
 
 static int run_device(gl_plan *pl, uint64_t *data, uint64_t count, bool inv, uint64_t *scratch,
                       cudaStream_t stream) {
-  return enqueue_transform(pl, data, data, 1, count, pl->size, inv, scratch, stream);
+  return gl_enqueue_transform(pl, data, data, 1, count, pl->size, inv, scratch, stream);
 }
 
 void gl_init_mempool_once() {
@@ -811,7 +819,7 @@ extern "C" int gl_ntt_columns(uint64_t *data, uint64_t rows, uint64_t cols, int 
   if (mem == GL_MEM_DEVICE) {
     gl_tmp tmp;
     if ((st = tmp.alloc(scratch, stream)) != GL_OK) return st;
-    return enqueue_transform(pl, data, data, cols, 1, len, dir == GL_INVERSE, tmp.u64(), stream);
+    return gl_enqueue_transform(pl, data, data, cols, 1, len, dir == GL_INVERSE, tmp.u64(), stream);
   }
   int st2 = GL_OK;
   {
@@ -819,7 +827,7 @@ extern "C" int gl_ntt_columns(uint64_t *data, uint64_t rows, uint64_t cols, int 
     if ((st = dbuf.alloc(len * sizeof(uint64_t) + scratch, stream)) != GL_OK) return st;
     cudaError_t e = cudaMemcpyAsync(dbuf.u64(), data, len * 8, cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return gl_cuda_status(e);
-    st = enqueue_transform(pl, dbuf.u64(), dbuf.u64(), cols, 1, len, dir == GL_INVERSE,
+    st = gl_enqueue_transform(pl, dbuf.u64(), dbuf.u64(), cols, 1, len, dir == GL_INVERSE,
                            scratch ? dbuf.u64() + len : nullptr, stream);
     if (st == GL_OK)
       st = gl_cuda_status(cudaMemcpyAsync(data, dbuf.u64(), len * 8, cudaMemcpyDeviceToHost, stream));
@@ -880,7 +888,7 @@ static int lde_device(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t co
   if (n == 1) {
     cudaError_t e = cudaMemcpyAsync(coef, in, nc * 8, cudaMemcpyDeviceToDevice, stream);
     if (e != cudaSuccess) return gl_cuda_status(e);
-  } else if ((st = enqueue_transform(pn, in, coef, cols, 1, nc, true, scr, stream)) != GL_OK) {
+  } else if ((st = gl_enqueue_transform(pn, in, coef, cols, 1, nc, true, scr, stream)) != GL_OK) {
     return st;
   }
   gl_load_opts lo;
@@ -891,7 +899,7 @@ static int lde_device(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t co
     cudaError_t e = cudaMemcpyAsync(out, coef, nc * 8, cudaMemcpyDeviceToDevice, stream);
     return gl_cuda_status(e);
   }
-  return enqueue_transform(pm, coef, out, cols, 1, mc, false, scr, stream, &lo);
+  return gl_enqueue_transform(pm, coef, out, cols, 1, mc, false, scr, stream, &lo);
 }
 
 extern "C" int gl_coset_lde(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t cols,

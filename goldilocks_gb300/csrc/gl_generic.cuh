@@ -37,6 +37,7 @@ __host__ __device__ __forceinline__ int gl_gen_ls(int m) { return ((m + 15) / 16
 struct gl_gen_ctx {
   const uint64_t *in;
   uint64_t *out;
+  const uint64_t *mul;  // GL_PF_OUT_MUL factors of this batch item
   int64_t lane0;
   int M, S1, LS, NR, R1, R2, R3;
 };
@@ -80,6 +81,7 @@ __device__ __forceinline__ void gl_gen_round1(const gl_pass_args &a, const gl_ge
         for (int t = 0; t < R; t++) {
           uint64_t v = scale_all ? gl_mul(x[t], a.tw_m[0]) : x[t];
           if (a.flags & GL_PF_PASS_TWIDDLE) v = gl_mul(v, gl_pass_tw(a, col, t));
+          if (a.flags & GL_PF_OUT_MUL) v = gl_out_mul(a, q.mul, lane, t, v);
           dst[(int64_t)t * a.out_is] = v;
         }
       }
@@ -149,6 +151,7 @@ __device__ __forceinline__ void gl_gen_round_last(const gl_pass_args &a, const g
         const uint64_t k = (uint64_t)(kbase + SL * t);
         uint64_t v = x[t];
         if (a.flags & GL_PF_PASS_TWIDDLE) v = gl_mul(v, gl_pass_tw(a, col, k));
+        if (a.flags & GL_PF_OUT_MUL) v = gl_out_mul(a, q.mul, lane, (int64_t)k, v);
         dst[(int64_t)k * a.out_is] = v;
       }
     }
@@ -169,6 +172,7 @@ __global__ void __launch_bounds__(GL_GEN_NT) gl_generic_kernel(const gl_pass_arg
   const bool ptr_table = (a.flags & GL_PF_PTR_TABLE) != 0;
   q.in = ptr_table ? a.in_ptrs[by] + bz * a.in_bs2 : a.in + by * a.in_bs + bz * a.in_bs2;
   q.out = ptr_table ? a.out_ptrs[by] + bz * a.out_bs2 : a.out + by * a.out_bs + bz * a.out_bs2;
+  q.mul = a.mul + by * a.mul_bs + bz * a.mul_bs2;
 
   GL_GEN_DISPATCH(q.R1, gl_gen_round1, a, q, sm)
   if (q.NR == 1) return;  // uniform across the CTA

@@ -83,6 +83,30 @@ void gl_launch(const gl_kernel_entry *k, int role, const gl_pass_args &a, dim3 g
 int gl_cuda_status(cudaError_t e);
 void gl_init_mempool_once();
 
+// Optional load-side transformation (the LDE's zero padding and coset shift).
+struct gl_load_opts {
+  uint32_t in_limit = 0xffffffffu;   // rows >= in_limit read as zero
+  const uint64_t *itw_lo = nullptr;  // g^e, e < 4096
+  const uint64_t *itw_hi = nullptr;  // g^(4096 e)
+};
+
+// Optional store-side pointwise product on the last pass of a forward
+// transform of contiguous sequences (C = 1): X_k *= factors[item*n + k], or
+// factors[k] for every item when `shared`; `mont` adds the factor 2^-64 that
+// makes it the product of two Montgomery words.
+struct gl_store_mul {
+  const uint64_t *factors = nullptr;
+  bool shared = false;
+  bool mont = false;
+};
+
+// Queue the transform of a strided batch on `stream`.  Element j of column c
+// of batch item b is at base[b*bs + j*C + c]; `src` and `dst` may be equal;
+// plans of two or three passes use `scratch` (>= n*C*B words).  (gl_api.cu)
+int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64_t C, uint64_t B,
+                         uint64_t bs, bool inv, uint64_t *scratch, cudaStream_t stream,
+                         const gl_load_opts *lo = nullptr, const gl_store_mul *om = nullptr);
+
 // Queue a batch on the persistent kernel without waiting; the kernel's error
 // word (0 = success) is copied to *err_out afterwards.  (gl_batch.cu)
 int gl_batch_enqueue_persistent(const gl_poly *polys, uint64_t count, cudaStream_t stream,

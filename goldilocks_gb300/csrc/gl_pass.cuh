@@ -29,6 +29,8 @@ enum : uint32_t {
   GL_PF_TW_TABLE = 32u,        // pass twiddle from tw_full[k*tw_ld + lane / tw_lane_div]
   GL_PF_LOAD_CG = 64u,         // read inputs through L2 only (written in the same launch)
   GL_PF_PTR_TABLE = 128u,      // batch item by = in_ptrs[by] / out_ptrs[by] (no *_bs)
+  GL_PF_OUT_MUL = 256u,        // final store: outputs *= mul[...] (pointwise spectrum product)
+  GL_PF_OUT_MUL_MONT = 512u,   // ... and * 2^-64 (product of two Montgomery words)
 };
 
 struct gl_pass_args {
@@ -54,6 +56,10 @@ struct gl_pass_args {
   const uint64_t *const *in_ptrs;  // GL_PF_PTR_TABLE: base pointer of batch item by
   uint64_t *const *out_ptrs;
   int32_t gen_r[3];                 // run-time radices of gl_generic_kernel
+  // GL_PF_OUT_MUL: the factor of output k of lane `lane` in batch item (by, bz)
+  // is mul[by*mul_bs + bz*mul_bs2 + lane*mul_ls + k*out_is].
+  const uint64_t *mul;
+  int64_t mul_ls, mul_bs, mul_bs2;
 };
 
 // Pass twiddle omega_n^(col*k): from the full table when present, else from
@@ -61,6 +67,13 @@ struct gl_pass_args {
 __device__ __forceinline__ uint64_t gl_pass_tw(const gl_pass_args &a, uint64_t col, uint64_t k) {
   if (a.flags & GL_PF_TW_TABLE) return __ldg(a.tw_full + (int64_t)k * a.tw_ld + (int64_t)col);
   return gl_mul(a.tw_lo[(col * k) & 4095], a.tw_hi[(col * k) >> 12]);
+}
+
+// Pointwise factor on the final store; `mb` is mul + by*mul_bs + bz*mul_bs2.
+__device__ __forceinline__ uint64_t gl_out_mul(const gl_pass_args &a, const uint64_t *mb,
+                                               int64_t lane, int64_t k, uint64_t v) {
+  v = gl_mul(v, __ldg(mb + lane * a.mul_ls + k * a.out_is));
+  return (a.flags & GL_PF_OUT_MUL_MONT) ? gl_shl<128>(v) : v;  // 2^128 = 2^-64
 }
 
 __device__ __forceinline__ uint64_t gl_tw2(const uint64_t *lo, const uint64_t *hi, uint64_t e) {
@@ -137,6 +150,11 @@ gl_pass_kernel(const gl_pass_args a) {
 #pragma unroll
         for (int kA = 0; kA < MA; kA++)
           dst[(int64_t)kA * a.out_is] = gl_mul(x[kA], gl_tw2(a.tw_lo, a.tw_hi, col * kA));
+      } else if (a.flags & GL_PF_OUT_MUL) {
+        const uint64_t *mb = a.mul + blockIdx.y * a.mul_bs + blockIdx.z * a.mul_bs2;
+#pragma unroll
+        for (int kA = 0; kA < MA; kA++)
+          dst[(int64_t)kA * a.out_is] = gl_out_mul(a, mb, lane0 + c, kA, x[kA]);
       } else {
 #pragma unroll
         for (int kA = 0; kA < MA; kA++) dst[(int64_t)kA * a.out_is] = x[kA];
@@ -167,6 +185,11 @@ gl_pass_kernel(const gl_pass_args a) {
             const uint64_t k = (uint64_t)(kA + MA * kB);
             dst[(int64_t)k * a.out_is] = gl_mul(y[kB], gl_tw2(a.tw_lo, a.tw_hi, col * k));
           }
+        } else if (a.flags & GL_PF_OUT_MUL) {
+          const uint64_t *mb = a.mul + blockIdx.y * a.mul_bs + blockIdx.z * a.mul_bs2;
+#pragma unroll
+          for (int kB = 0; kB < MB; kB++)
+            dst[(int64_t)(kA + MA * kB) * a.out_is] = gl_out_mul(a, mb, lane, kA + MA * kB, y[kB]);
         } else {
 #pragma unroll
           for (int kB = 0; kB < MB; kB++) dst[(int64_t)(kA + MA * kB) * a.out_is] = y[kB];

@@ -105,6 +105,10 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
 #pragma unroll
             for (int t = 0; t < R1; t++)
               dst[(int64_t)t * a.out_is] = gl_mul(x[t], gl_pass_tw(a, col, t));
+          } else if (a.flags & GL_PF_OUT_MUL) {
+            const uint64_t *mb = a.mul + by * a.mul_bs + bz * a.mul_bs2;
+#pragma unroll
+            for (int t = 0; t < R1; t++) dst[(int64_t)t * a.out_is] = gl_out_mul(a, mb, lane, t, x[t]);
           } else {
 #pragma unroll
             for (int t = 0; t < R1; t++) dst[(int64_t)t * a.out_is] = x[t];
@@ -178,6 +182,11 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
             const uint64_t k = (uint64_t)(kbase + SL * t);
             dst[(int64_t)k * a.out_is] = gl_mul(x[t], gl_pass_tw(a, col, k));
           }
+        } else if (a.flags & GL_PF_OUT_MUL) {
+          const uint64_t *mb = a.mul + by * a.mul_bs + bz * a.mul_bs2;
+#pragma unroll
+          for (int t = 0; t < RL; t++)
+            dst[(int64_t)(kbase + SL * t) * a.out_is] = gl_out_mul(a, mb, lane, kbase + SL * t, x[t]);
         } else {
 #pragma unroll
           for (int t = 0; t < RL; t++) dst[(int64_t)(kbase + SL * t) * a.out_is] = x[t];

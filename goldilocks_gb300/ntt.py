@@ -133,6 +133,28 @@ def intt(values):
     return values
 
 
+def convolve(a, b_hat, size=None, montgomery=True):
+    """convolve::circular (ntt/src/convolve.rs:13-20): a <- intt(ntt(a) * b_hat)
+    in place, for each length-`size` sequence of `a` (default: all of `a`).
+    `b_hat` (already in NTT form) holds one sequence shared by all, or one per
+    sequence.  `montgomery`: words are the reference's Field words (the
+    product is a*b*2^-64); False: canonical values."""
+    ptr, n, mem, stream = _buffer(a)
+    bptr, bn, bmem, _ = _buffer(b_hat)
+    if bmem != mem:
+        raise ValueError("a and b_hat must both be host arrays or both device tensors")
+    size = n if size is None else size
+    if size == 0 or n % size:
+        _check(L.GL_ERR_UNSUPPORTED_SIZE if size == 0 else L.GL_ERR_INVALID, "convolve", size=size)
+    count = n // size
+    if bn % size or bn // size not in (1, count):
+        raise ValueError("b_hat must hold one sequence or one per sequence of a")
+    repr_ = L.GL_REPR_MONTGOMERY if montgomery else L.GL_REPR_CANONICAL
+    _check(L.load().gl_convolve(ptr, bptr, size, count, bn // size, repr_, mem, stream),
+           "convolve", size=size)
+    return a
+
+
 def clear_cache():
     L.load().gl_clear_cache()
 

@@ -118,6 +118,25 @@ int gl_ntt_columns(uint64_t *data, uint64_t rows, uint64_t cols, int dir, int me
 int gl_coset_lde(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t cols, uint32_t blowup,
                  uint64_t shift, int mem, void *stream);
 
+/* ---- circular convolution (ntt/src/convolve.rs:13-20) ---- */
+
+enum { GL_REPR_CANONICAL = 0, GL_REPR_MONTGOMERY = 1 };
+
+/* Replaces convolve::circular(a, b) (ntt/src/convolve.rs:13-20): for each of
+ * the `count` contiguous length-n sequences of `a`, a <- intt(ntt(a) * b_hat)
+ * in place, where b_hat is already in NTT form.  `b_count` is 1 (one b_hat of
+ * n words for every sequence) or `count` (one per sequence, contiguous).
+ *
+ * Unlike the transforms, the pointwise product depends on the representation:
+ * `repr` = GL_REPR_MONTGOMERY multiplies words as the reference's Field does
+ * (Montgomery product a*b*2^-64, ntt/src/field/mod.rs:12), GL_REPR_CANONICAL
+ * multiplies canonical values.  The product is fused into the last pass of
+ * the forward transform.  Both buffers in device memory (GL_MEM_DEVICE, queued
+ * on `stream`) or both in host memory (synchronous).  n = 0 and non-divisors
+ * of p - 1: GL_ERR_UNSUPPORTED_SIZE (the reference panics in ntt()). */
+int gl_convolve(uint64_t *a, const uint64_t *b_hat, uint64_t n, uint64_t count, uint64_t b_count,
+                int repr, int mem, void *stream);
+
 /* ---- batches of polynomials of uneven lengths (no counterpart in the reference) ---- */
 
 typedef struct {

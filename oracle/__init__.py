@@ -73,6 +73,7 @@ def lib():
         l.glo_strategy_describe.argtypes = [_u64, ctypes.c_char_p, ctypes.c_size_t]
         l.glo_coset_lde.argtypes = [_vp, _vp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_uint32, _u64]
         l.glo_convolve.argtypes = [_vp, _vp, ctypes.c_size_t]
+        l.glo_convolve_mont.argtypes = [_vp, _vp, ctypes.c_size_t]
         _lib = l
     return _lib
 
@@ -120,6 +121,35 @@ def coset_lde(x, n, cols, blowup, shift):
     if lib().glo_coset_lde(x.ctypes.data, out.ctypes.data, n, cols, blowup, shift):
         raise ValueError("oracle: unsupported LDE shape")
     return out
+
+
+def convolve(a, b_hat, size=None, montgomery=True):
+    """Per length-`size` sequence of a: intt(ntt(a) * b_hat); b_hat holds one
+    sequence for all or one per sequence; Montgomery or canonical product."""
+    y = _arr(a).copy()
+    b = _arr(b_hat)
+    size = y.size if size is None else size
+    f = lib().glo_convolve_mont if montgomery else lib().glo_convolve
+    for i in range(y.size // size):
+        seg = y[i * size:(i + 1) * size]
+        bs = b if b.size == size else b[i * size:(i + 1) * size]
+        bs = np.ascontiguousarray(bs)
+        if size == 1:  # ntt and intt of one element are the identity
+            seg[0] = lib().glo_from_mont(int(seg[0]) * int(bs[0]) % P) if montgomery else \
+                int(seg[0]) * int(bs[0]) % P
+        elif f(seg.ctypes.data, bs.ctypes.data, size):
+            raise ValueError("oracle: unsupported size")
+    return y
+
+
+def to_mont(x):
+    """Field::new of each value: x*2^64 mod p."""
+    return np.array([lib().glo_to_mont(int(v)) for v in _arr(x)], dtype=np.uint64)
+
+
+def from_mont(x):
+    """u64::from(Field) of each word: x*2^-64 mod p."""
+    return np.array([lib().glo_from_mont(int(v)) for v in _arr(x)], dtype=np.uint64)
 
 
 def strategy_describe(size):

@@ -481,3 +481,12 @@ int glo_convolve(uint64_t *a, const uint64_t *b_hat, size_t n) {
     for (size_t i = 0; i < n; i++) a[i] = o_mul(a[i], b_hat[i]);
     return glo_intt(a, n);
 }
+
+int glo_convolve_mont(uint64_t *a, const uint64_t *b_hat, size_t n) {
+    if (glo_ntt(a, n)) return -1;
+    for (size_t i = 0; i < n; i++) {
+        uint64_t v = o_mont_reduce_128((o_u128)a[i] * b_hat[i]);
+        a[i] = v >= O_P ? v - O_P : v;
+    }
+    return glo_intt(a, n);
+}

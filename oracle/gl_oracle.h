@@ -46,8 +46,14 @@ int glo_strategy_describe(uint64_t size, char *buf, size_t cap);
 int glo_coset_lde(const uint64_t *in, uint64_t *out, size_t n, size_t cols,
                   uint32_t blowup, uint64_t shift);
 
-/* Circular convolution (convolve.rs:13-20): a <- intt(ntt(a) * b_hat). */
+/* Circular convolution (convolve.rs:13-20): a <- intt(ntt(a) * b_hat), the
+ * pointwise product of canonical values. */
 int glo_convolve(uint64_t *a, const uint64_t *b_hat, size_t n);
+
+/* The same on the reference's Field words: the pointwise product is the
+ * Montgomery product a*b*2^-64 (Field's MulAssign, field/mod.rs, reduced as
+ * field/algo/generic.rs does); the transforms are the same linear maps. */
+int glo_convolve_mont(uint64_t *a, const uint64_t *b_hat, size_t n);
 
 #ifdef __cplusplus
 }

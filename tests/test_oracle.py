@@ -55,6 +55,10 @@ def test_reference_kats(oracle):
     bh = oracle.ntt(np.array(c["b"], dtype=np.uint64))
     lib.glo_convolve(a.ctypes.data, bh.ctypes.data, 3)
     assert a.tolist() == c["c"]
+    # The same KAT on Field (Montgomery) words, as the reference's test runs it.
+    am = oracle.to_mont(c["a"])
+    bm = oracle.ntt(oracle.to_mont(c["b"]))
+    assert oracle.from_mont(oracle.convolve(am, bm, montgomery=True)).tolist() == c["c"]
 
 
 def test_split_all_divisors(oracle):
