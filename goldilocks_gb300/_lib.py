@@ -36,6 +36,14 @@ SIGNATURES = [
     ("gl_ntt_columns", _int, [_vp, _u64, _u64, _int, _int, _vp]),
     ("gl_coset_lde", _int, [_vp, _vp, _u64, _u64, _u32, _u64, _int, _vp]),
     ("gl_convolve", _int, [_vp, _vp, _u64, _u64, _u64, _int, _int, _vp]),
+    ("gl_k12_next_layer_size", _u64, [_u64]),
+    ("gl_merkle_tree_bytes", _u64, [_u64]),
+    ("gl_k12_process_layer", _int, [_vp, _u64, _vp, _int, _vp]),
+    ("gl_k12_hash_many", _int, [_vp, _u64, _u64, _vp, _u32, _int, _vp]),
+    ("gl_merkle_tree", _int, [_vp, _u64, _vp, _u64, _int, _vp]),
+    ("gl_pow_hashes", _int, [_vp, _u64, _u64, _vp, _int, _vp]),
+    ("gl_pow_verify", _int, [_vp, _u64, _u64, ctypes.POINTER(_int), _vp]),
+    ("gl_pow_solve", _int, [_vp, _u64, _u64, _u64, _u64p, _vp]),
     ("gl_batch_execute", _int, [_vp, _u64, _int, _vp]),
     ("gl_batch_autotune", _int, [_vp, _u64, _int, _vp, _vp]),
     ("gl_server_create", _int, [_u64, _int, _int, ctypes.POINTER(_vp)]),

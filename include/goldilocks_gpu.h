@@ -137,6 +137,42 @@ enum { GL_REPR_CANONICAL = 0, GL_REPR_MONTGOMERY = 1 };
 int gl_convolve(uint64_t *a, const uint64_t *b_hat, uint64_t n, uint64_t count, uint64_t b_count,
                 int repr, int mem, void *stream);
 
+/* ---- K12 Merkle layers and proof of work (pcs/src/k12, pcs/src/pow.rs) ----
+ *
+ * Byte-oriented; `mem` applies to every data buffer of a call (the 32-byte
+ * challenge and the results of gl_pow_verify / gl_pow_solve are host memory).
+ * Hashes are single-block KangarooTwelve (pcs/src/k12/generic.rs:62-84) with
+ * 32-byte outputs over 160-byte blocks (pcs/src/k12/mod.rs:28-29). */
+
+/* next_layer_size (pcs/src/k12/mod.rs:33-35): ceil(size / 160) * 32. */
+uint64_t gl_k12_next_layer_size(uint64_t size);
+/* Total bytes of all layers merkle_tree produces for `len` input bytes. */
+uint64_t gl_merkle_tree_bytes(uint64_t len);
+/* process_layer (pcs/src/k12/generic.rs:86-95): each 160-byte block of in
+ * (the last may be shorter) hashed to 32 bytes of out. */
+int gl_k12_process_layer(const uint8_t *in, uint64_t len, uint8_t *out, int mem, void *stream);
+/* k12::<out_len> (generic.rs:62-84) of `count` messages of msg_len bytes
+ * stored back to back: msg_len <= 166, out_len <= 168, else GL_ERR_INVALID. */
+int gl_k12_hash_many(const uint8_t *in, uint64_t msg_len, uint64_t count, uint8_t *out,
+                     uint32_t out_len, int mem, void *stream);
+/* merkle_tree (pcs/src/k12/mod.rs:41-60): layers of process_layer until one is
+ * at most 32 bytes, written back to back into `layers` (first layer first,
+ * the 32-byte root last); layers_bytes >= gl_merkle_tree_bytes(len). */
+int gl_merkle_tree(const uint8_t *values, uint64_t len, uint8_t *layers, uint64_t layers_bytes,
+                   int mem, void *stream);
+/* out[i] = the proof-of-work hash of nonce start + i: the first 8 bytes,
+ * little endian, of k12(challenge || nonce as 8 little-endian bytes)
+ * (pcs/src/pow.rs:32-37; k12_pow_2, pcs/src/k12/aarch64.rs:92). */
+int gl_pow_hashes(const uint8_t *challenge, uint64_t start, uint64_t count, uint64_t *out, int mem,
+                  void *stream);
+/* Pow::verify (pow.rs:32-37): *ok = hash(nonce) >= threshold.  Synchronous. */
+int gl_pow_verify(const uint8_t *challenge, uint64_t threshold, uint64_t nonce, int *ok, void *stream);
+/* Pow::solve (pow.rs:39-60) over a bounded range: the smallest nonce in
+ * [start, start + max_count) with hash >= threshold, or GL_ERR_NOT_FOUND.
+ * Synchronous; the reference searches from 0 without bound. */
+int gl_pow_solve(const uint8_t *challenge, uint64_t threshold, uint64_t start, uint64_t max_count,
+                 uint64_t *nonce, void *stream);
+
 /* ---- batches of polynomials of uneven lengths (no counterpart in the reference) ---- */
 
 typedef struct {

@@ -1,7 +1,8 @@
 """CPU oracle for the Goldilocks NTT path -- TEST INFRASTRUCTURE ONLY.
 
 A C restatement of recmo/goldilocks' `goldilocks-ntt` transform path
-(gl_oracle.c, codelets_gen.c from codegen_ref.py), loaded through ctypes.
+(gl_oracle.c, codelets_gen.c from codegen_ref.py) and of the `goldilocks-pcs`
+K12 Merkle layers and proof of work (k12_oracle.c), loaded through ctypes.
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it,
 as the checker; the product (goldilocks_gb300/) never does.
 
@@ -18,7 +19,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgl_oracle.so")
-SOURCES = [os.path.join(HERE, "gl_oracle.c"), os.path.join(HERE, "codelets_gen.c")]
+SOURCES = [os.path.join(HERE, "gl_oracle.c"), os.path.join(HERE, "codelets_gen.c"),
+           os.path.join(HERE, "k12_oracle.c")]
 P = 0xFFFF_FFFF_0000_0001
 
 
@@ -74,6 +76,15 @@ def lib():
         l.glo_coset_lde.argtypes = [_vp, _vp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_uint32, _u64]
         l.glo_convolve.argtypes = [_vp, _vp, ctypes.c_size_t]
         l.glo_convolve_mont.argtypes = [_vp, _vp, ctypes.c_size_t]
+        l.glo_k12.argtypes = [_vp, ctypes.c_size_t, _vp, ctypes.c_size_t]
+        l.glo_k12_next_layer_size.restype = ctypes.c_size_t
+        l.glo_k12_next_layer_size.argtypes = [ctypes.c_size_t]
+        l.glo_k12_process_layer.argtypes = [_vp, ctypes.c_size_t, _vp]
+        l.glo_merkle_tree.restype = ctypes.c_size_t
+        l.glo_merkle_tree.argtypes = [_vp, ctypes.c_size_t, _vp, ctypes.c_size_t]
+        l.glo_pow_hash.restype = _u64
+        l.glo_pow_hash.argtypes = [_vp, _u64]
+        l.glo_pow_solve.argtypes = [_vp, _u64, _u64, _u64, ctypes.POINTER(_u64)]
         _lib = l
     return _lib
 
@@ -150,6 +161,49 @@ def to_mont(x):
 def from_mont(x):
     """u64::from(Field) of each word: x*2^-64 mod p."""
     return np.array([lib().glo_from_mont(int(v)) for v in _arr(x)], dtype=np.uint64)
+
+
+def k12(msg, out_len=32):
+    """k12::<out_len>(msg) for len(msg) <= 166 (pcs/src/k12/generic.rs:62-84)."""
+    m = np.frombuffer(bytes(msg), dtype=np.uint8).copy()
+    out = np.zeros(out_len, dtype=np.uint8)
+    if lib().glo_k12(m.ctypes.data if m.size else None, m.size, out.ctypes.data, out_len):
+        raise ValueError("oracle: k12 input longer than 166 bytes or output longer than 168")
+    return out.tobytes()
+
+
+def k12_process_layer(data):
+    d = np.frombuffer(bytes(data), dtype=np.uint8).copy()
+    out = np.zeros(lib().glo_k12_next_layer_size(d.size), dtype=np.uint8)
+    lib().glo_k12_process_layer(d.ctypes.data, d.size, out.ctypes.data)
+    return out.tobytes()
+
+
+def merkle_tree(values):
+    """The layers of merkle_tree (pcs/src/k12/mod.rs:41-60) as a list of bytes."""
+    v = np.frombuffer(bytes(values), dtype=np.uint8).copy()
+    total = lib().glo_merkle_tree(v.ctypes.data, v.size, None, 0)
+    out = np.zeros(max(total, 1), dtype=np.uint8)
+    lib().glo_merkle_tree(v.ctypes.data, v.size, out.ctypes.data, total)
+    layers, off, n = [], 0, v.size
+    while n > 32:
+        n = lib().glo_k12_next_layer_size(n)
+        layers.append(out[off:off + n].tobytes())
+        off += n
+    return layers
+
+
+def pow_hash(challenge, nonce):
+    c = np.frombuffer(bytes(challenge), dtype=np.uint8).copy()
+    return lib().glo_pow_hash(c.ctypes.data, nonce)
+
+
+def pow_solve(challenge, threshold, start=0, count=1 << 40):
+    c = np.frombuffer(bytes(challenge), dtype=np.uint8).copy()
+    n = _u64()
+    if lib().glo_pow_solve(c.ctypes.data, threshold, start, count, ctypes.byref(n)):
+        return None
+    return n.value
 
 
 def strategy_describe(size):

@@ -55,6 +55,16 @@ int glo_convolve(uint64_t *a, const uint64_t *b_hat, size_t n);
  * field/algo/generic.rs does); the transforms are the same linear maps. */
 int glo_convolve_mont(uint64_t *a, const uint64_t *b_hat, size_t n);
 
+/* ---- K12 hashing (k12_oracle.c; pcs/src/k12, pcs/src/pow.rs) ---- */
+void glo_keccak_p1600_12(uint64_t st[25]);
+int glo_k12(const uint8_t *in, size_t len, uint8_t *out, size_t h);
+size_t glo_k12_next_layer_size(size_t size);
+void glo_k12_process_layer(const uint8_t *in, size_t len, uint8_t *out);
+size_t glo_merkle_tree(const uint8_t *values, size_t len, uint8_t *out, size_t cap);
+uint64_t glo_pow_hash(const uint8_t challenge[32], uint64_t nonce);
+int glo_pow_solve(const uint8_t challenge[32], uint64_t threshold, uint64_t start, uint64_t count,
+                  uint64_t *nonce);
+
 #ifdef __cplusplus
 }
 #endif

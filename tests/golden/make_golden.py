@@ -13,6 +13,9 @@ Writes:
   dft_vectors.json        -- seeded inputs and their O(n^2) DFT computed here with
                              Python integers (independent of any C code), for a set
                              of small sizes including the reference test sizes.
+  k12_kats.json           -- the K12 and proof-of-work known answers of the pcs
+                             crate's unit tests (pcs/src/k12/generic.rs,
+                             pcs/src/k12/aarch64.rs, pcs/src/pow.rs).
 """
 import json
 import os
@@ -72,6 +75,65 @@ def kats(ref):
     }
 
 
+def k12_kats(ref):
+    def read(p):
+        return open(os.path.join(ref, p)).read()
+
+    gen = read("pcs/src/k12/generic.rs")
+    hashes = []
+    for name, body in re.findall(r"fn (test_\w+)\(\) \{(.*?)\n    \}", gen, re.S):
+        m = re.search(r"k12::<(\d+)>", body)
+        h = re.search(r'to_hex\(&actual\[\.\.\]\),\s*"([^"]*)"', body, re.S)
+        if not m or not h:
+            continue  # property tests against other libraries
+        z = re.search(r"let mut input = \[0u8; (\d+)\];", body)
+        pat = re.search(r"\(0\.\.0xfa\)\.cycle\(\)\.take\((\d+)\)", body)
+        if z:
+            msg = [0] * int(z.group(1))
+        elif pat:
+            msg = [i % 0xFA for i in range(int(pat.group(1)))]
+        else:
+            raise ValueError("unrecognised K12 test input in " + name)
+        hexstr = re.sub(r"\\\s*\n\s*", " ", h.group(1)).replace(" ", "")
+        hashes.append({"name": name, "input": msg, "out_len": int(m.group(1)), "hash": hexstr})
+
+    pow_src = read("pcs/src/pow.rs")
+    verify = []
+    for name, body in re.findall(r"fn (test_pow_[01])\(\) \{(.*?)\n    \}", pow_src, re.S):
+        ch = int(re.search(r"\[0x([0-9a-f]+)_u8; 32\]", body).group(1), 16)
+        thr = re.search(r"Pow::new\(challenge, ([^)]+)\)", body).group(1).strip()
+        thr = 1 << int(thr.split("<<")[1]) if "<<" in thr else int(thr)
+        for neg, nonce in re.findall(r"assert!\((!?)pow\.verify\((\d+)\)\);", body):
+            verify.append({"challenge_byte": ch, "threshold": thr, "nonce": int(nonce),
+                           "ok": neg != "!"})
+    solve = []
+    for name, body in re.findall(r"fn (test_pow_solve\w*)\(\) \{(.*?)\n    \}", pow_src, re.S):
+        ch = int(re.search(r"\[0x([0-9a-f]+)_u8; 32\]", body).group(1), 16)
+        thr = re.search(r"Pow::new\(challenge, (.*)\);", body).group(1).strip()
+        bits = re.search(r"threshold_from_bits\(([\d.]+)\)", thr)
+        if bits:
+            # pow.rs:16-18: u64::MAX - 2^(64 - bits) (exact for integer bits)
+            t = (1 << 64) - 1 - (1 << (64 - int(float(bits.group(1)))))
+        else:
+            t = 1 << int(thr.split("<<")[1])
+        nonce = int(re.search(r"assert_eq!\(pow\.solve\(\), (\d+)\);", body).group(1))
+        solve.append({"name": name, "challenge_byte": ch, "threshold": t,
+                      "bits": float(bits.group(1)) if bits else None, "nonce": nonce})
+    a64 = read("pcs/src/k12/aarch64.rs")
+    body = re.search(r"fn test_pow_d\(\) \{(.*?)\n    \}", a64, re.S).group(1)
+    ch = int(re.search(r"\[0x([0-9a-f]+); 32\]", body).group(1), 16)
+    n0, n1 = re.search(r"k12_pow_2\(&challenge, ([^,]+), ([^)]+)\)", body).groups()
+    nn = lambda v: (1 << 64) - 1 if v.strip() == "u64::MAX" else int(v)
+    outs = [int(v) for v in re.findall(r"assert_eq!\([ab], (\d+)\);", body)]
+    pow_hashes = [{"challenge_byte": ch, "nonce": nn(n0), "hash": outs[0]},
+                  {"challenge_byte": ch, "nonce": nn(n1), "hash": outs[1]}]
+    return {"k12": {"cases": hashes, "source": "pcs/src/k12/generic.rs:113-162"},
+            "pow_verify": {"cases": verify, "source": "pcs/src/pow.rs:67-85"},
+            "pow_solve": {"cases": solve, "source": "pcs/src/pow.rs:87-107"},
+            "pow_hash": {"cases": pow_hashes, "source": "pcs/src/k12/aarch64.rs:234-240"},
+            "layer": {"block_size": 160, "hash_size": 32, "source": "pcs/src/k12/mod.rs:28-29"}}
+
+
 def splitmix64(x):
     x = (x + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
     z = x
@@ -118,6 +180,8 @@ def main():
         json.dump(kats(ref), f, indent=1)
     with open(os.path.join(HERE, "dft_vectors.json"), "w") as f:
         json.dump(dft_vectors(), f)
+    with open(os.path.join(HERE, "k12_kats.json"), "w") as f:
+        json.dump(k12_kats(ref), f, indent=1)
 
 
 if __name__ == "__main__":
