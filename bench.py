@@ -219,6 +219,97 @@ def bench_serving(gl, torch, count=300, log_max=20):
     return res
 
 
+def _time_ms(torch, fn, reps):
+    stream = torch.cuda.current_stream()
+    fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        fn()
+    b.record(stream)
+    b.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def bench_commit(gl, torch, reps=3):
+    """Config 4 and the step after it: coset LDE of a 2^20 x 256 row-major
+    matrix (blowup 4, shift 7) to 2^22 x 256, then the K12 Merkle tree of the
+    8 GiB result (pcs/src/k12/mod.rs:41-60)."""
+    import numpy as np
+    from goldilocks_gb300 import _lib as L
+    lib = L.load()
+    n, cols, blowup = 1 << 20, 256, 4
+    s = torch.cuda.current_stream().cuda_stream
+    inp = torch.from_numpy(gl.fill_uniform(n * cols, seed=0xC0417).view(np.int64)).cuda()
+    out = torch.empty(n * blowup * cols, dtype=torch.int64, device="cuda")
+    leaves = out.numel() * 8
+    tree_bytes = lib.gl_merkle_tree_bytes(leaves)
+    tree = torch.empty(tree_bytes, dtype=torch.uint8, device="cuda")
+
+    def lde():
+        assert lib.gl_coset_lde(inp.data_ptr(), out.data_ptr(), n, cols, blowup, 7, L.GL_MEM_DEVICE, s) == 0
+
+    def merkle():
+        assert lib.gl_merkle_tree(out.data_ptr(), leaves, tree.data_ptr(), tree_bytes, L.GL_MEM_DEVICE, s) == 0
+
+    lde_ms = _time_ms(torch, lde, reps)
+    merkle_ms = _time_ms(torch, merkle, reps)
+    import math
+    alg = cols * sum(16 * m * math.ceil(math.log2(m) / 14) for m in (n, n * blowup))
+    res = {"shape": "2^20 x 256 -> 2^22 x 256, blowup 4, shift 7",
+           "lde_ms": lde_ms, "lde_rows_cols_per_s": n * cols / (lde_ms * 1e-3),
+           "lde_algorithmic_gbs": alg / (lde_ms * 1e-3) / 1e9,
+           "merkle_ms": merkle_ms, "merkle_leaf_bytes": leaves,
+           "merkle_leaf_gbs": leaves / (merkle_ms * 1e-3) / 1e9,
+           "merkle_permutations_per_s": (leaves + tree_bytes) / 160 / (merkle_ms * 1e-3),
+           "commit_ms": lde_ms + merkle_ms}
+    del inp, out, tree
+    torch.cuda.empty_cache()
+    return res
+
+
+def bench_convolve(gl, torch, reps=5):
+    """convolve::circular at n = 2^24 (ntt, fused pointwise product, intt)."""
+    import numpy as np
+    n = 1 << 24
+    a = torch.from_numpy(gl.fill_uniform(n, seed=0xC011).view(np.int64)).cuda()
+    b = torch.from_numpy(gl.fill_uniform(n, seed=0xC012).view(np.int64)).cuda()
+    ms = _time_ms(torch, lambda: gl.convolve(a, b), reps)
+    return {"n": n, "ms": ms, "elem_s": n / (ms * 1e-3), "repr": "montgomery"}
+
+
+def bench_pow(torch):
+    """Pow::solve (pcs/src/pow.rs:39-60): the reference's 32-bit case
+    (challenge 0xaa * 32, answer 440258853) and the raw hash rate over 2^33
+    nonces with a threshold nothing meets."""
+    from goldilocks_gb300.k12 import Pow
+    p = Pow(bytes([0xAA] * 32), Pow.threshold_from_bits(32.0))
+    p.solve()
+    t = time.perf_counter()
+    nonce = p.solve()
+    solve_s = time.perf_counter() - t
+    scan = Pow(bytes([0x11] * 32), 2**64 - 1)
+    t = time.perf_counter()
+    scan.solve(max_count=1 << 33)
+    scan_s = time.perf_counter() - t
+    return {"solve_32bit_nonce": nonce, "solve_32bit_s": solve_s,
+            "hashes_per_s": (1 << 33) / scan_s}
+
+
+def cpu_oracle_k12_rate(seconds=2.0):
+    """Single-thread rate of the K12 oracle (C restatement of
+    pcs/src/k12/generic.rs) on 160-byte blocks."""
+    import oracle
+    data = bytes(range(256)) * 640  # 1024 blocks
+    oracle.k12_process_layer(data)
+    t, reps = time.perf_counter(), 0
+    while time.perf_counter() - t < seconds:
+        oracle.k12_process_layer(data)
+        reps += 1
+    return reps * 1024 / (time.perf_counter() - t)
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -359,6 +450,17 @@ def run_ours(args):
             line["serving"] = bench_serving(gl, torch)
         except Exception as e:
             line["serving"] = {"error": str(e)}
+        for key, fn in (("commit", lambda: bench_commit(gl, torch)),
+                        ("convolve", lambda: bench_convolve(gl, torch)),
+                        ("pow", lambda: bench_pow(torch))):
+            try:
+                line[key] = fn()
+            except Exception as e:
+                line[key] = {"error": str(e)}
+        if not args.no_cpu_baseline:
+            k12_rate = cpu_oracle_k12_rate()
+            line["commit"]["cpu_oracle_k12_blocks_per_s_1_thread"] = k12_rate
+            line["pow"]["cpu_oracle_hashes_per_s_1_thread"] = k12_rate
     if world == 1 and not args.no_cpu_baseline:
         threads = min(2 * len(SIZES), os.cpu_count() or 1)
         el, s = cpu_oracle_step(threads)
@@ -378,7 +480,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-extras", action="store_true", help="skip the batched and serving figures")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched, serving, commit, convolve and proof-of-work figures")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
