@@ -322,7 +322,9 @@ int gl_plan_tables(gl_plan *pl, gl_dev_tables **out) {
   gl_dev_tables t;
   int st = GL_OK;
   const uint64_t n = pl->size;
-  if (pl->kind == 1) {
+  if (pl->kind == 4) {
+    st = gl_rader_tables(pl, t);
+  } else if (pl->kind == 1) {
     for (int d = 0; d < 2 && st == GL_OK; d++)
       st = upload(t, powers(h_root(n, d), n, 1), &t.blk[0][d]);
     if (st == GL_OK) st = upload(t, powers(h_root(n, true), n, gl_inv(n % GL_P)), &t.blk_scaled_inv);
@@ -378,20 +380,49 @@ extern "C" int gl_plan_create(uint64_t size, gl_plan **out) {
   if (!out) return GL_ERR_INVALID;
   *out = nullptr;
   if (!gl_is_divisor(size)) return GL_ERR_UNSUPPORTED_SIZE;
-  std::lock_guard<std::mutex> lk(g_cache_mu);
-  auto it = g_cache.find(size);
-  if (it != g_cache.end()) { *out = it->second; return GL_OK; }
+  {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    auto it = g_cache.find(size);
+    if (it != g_cache.end()) { *out = it->second; return GL_OK; }
+  }
   gl_plan *pl = new gl_plan();
   pl->size = size;
   pl->tree = reference_tree(size);
-  choose_schedule(pl);
+  // A factor 65537 or 257 takes a Rader step (gl_rader.cu); its sub-plans are
+  // made first, outside the cache lock.
+  const uint64_t q = size % 65537 == 0 ? 65537 : size % 257 == 0 ? 257 : 0;
+  if (q) {
+    int st = gl_plan_create(q - 1, &pl->pq);
+    if (st == GL_OK) st = gl_plan_create(size / q, &pl->pm);
+    if (st != GL_OK) {
+      delete pl;
+      return st;
+    }
+    pl->kind = 4;
+    pl->q = q;
+  } else {
+    choose_schedule(pl);
+  }
   if (pl->kind < 0) {
     delete pl;
     return GL_ERR_UNSUPPORTED_SIZE;
   }
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  auto it = g_cache.find(size);
+  if (it != g_cache.end()) {  // another thread made it meanwhile
+    delete pl;
+    *out = it->second;
+    return GL_OK;
+  }
   g_cache[size] = pl;
   *out = pl;
   return GL_OK;
+}
+
+uint64_t gl_plan_scratch_words(const gl_plan *pl, uint64_t C, uint64_t B) {
+  if (!pl || pl->kind <= 1) return 0;
+  if (pl->kind == 4) return gl_rader_scratch_words(pl, C);  // items run one after another
+  return pl->size * C * B;
 }
 
 // Plans are shared and immutable once built; a cleared cache forgets them
@@ -414,9 +445,16 @@ extern "C" int gl_plan_describe(const gl_plan *plan, char *buf, size_t cap) {
   if (plan->kind == 0) s += "no-op";
   else if (plan->kind == 1) s += "full " + kname(plan->k[0][0]);
   else if (plan->kind == 2) s += "col " + kname(plan->k[0][0]) + " + row " + kname(plan->k[1][0]);
-  else
+  else if (plan->kind == 3)
     s += "col " + kname(plan->k[0][0]) + " + col " + kname(plan->k[1][0]) + " + row " +
          kname(plan->k[2][0]);
+  else {
+    char sub[1024];
+    s += "rader " + std::to_string(plan->q) + " [conv " + std::to_string(plan->q - 1);
+    if (gl_plan_describe(plan->pq, sub, sizeof sub) == GL_OK) s += ": " + std::string(strstr(sub, "gpu: ") + 5);
+    s += "] then " + std::to_string(plan->size / plan->q);
+    if (gl_plan_describe(plan->pm, sub, sizeof sub) == GL_OK) s += ": " + std::string(strstr(sub, "gpu: ") + 5);
+  }
   size_t n = std::min(cap - 1, s.size());
   memcpy(buf, s.data(), n);
   buf[n] = 0;
@@ -424,8 +462,7 @@ extern "C" int gl_plan_describe(const gl_plan *plan, char *buf, size_t cap) {
 }
 
 extern "C" uint64_t gl_plan_workspace_bytes(const gl_plan *plan, uint64_t count) {
-  if (!plan || plan->kind < 2) return 0;
-  return plan->size * count * sizeof(uint64_t);
+  return gl_plan_scratch_words(plan, 1, count) * sizeof(uint64_t);
 }
 
 // ---------------------------------------------------------------- profiling
@@ -510,6 +547,10 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
   gl_load_opts none;
   if (!lo) lo = &none;
   if (om && (C != 1 || pl->kind == 0)) return GL_ERR_INVALID;  // contiguous transforms only
+  if (pl->kind == 4) {
+    if (om || lo->itw_lo || lo->in_limit != 0xffffffffu) return GL_ERR_INVALID;
+    return gl_rader_enqueue(pl, src, dst, C, B, bs, inv, scratch, stream);
+  }
   const uint32_t mul_flags = om ? (GL_PF_OUT_MUL | (om->mont ? GL_PF_OUT_MUL_MONT : 0u)) : 0u;
   const int64_t mul_item = om && !om->shared ? (int64_t)n : 0;  // factor stride per item
   if (pl->kind == 0) {
@@ -815,7 +856,7 @@ extern "C" int gl_ntt_columns(uint64_t *data, uint64_t rows, uint64_t cols, int 
   if (st != GL_OK) return st;
   gl_init_mempool_once();
   const uint64_t len = rows * cols;
-  const size_t scratch = pl->kind >= 2 ? len * sizeof(uint64_t) : 0;
+  const size_t scratch = gl_plan_scratch_words(pl, cols, 1) * sizeof(uint64_t);
   if (mem == GL_MEM_DEVICE) {
     gl_tmp tmp;
     if ((st = tmp.alloc(scratch, stream)) != GL_OK) return st;
@@ -828,7 +869,7 @@ extern "C" int gl_ntt_columns(uint64_t *data, uint64_t rows, uint64_t cols, int 
     cudaError_t e = cudaMemcpyAsync(dbuf.u64(), data, len * 8, cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return gl_cuda_status(e);
     st = gl_enqueue_transform(pl, dbuf.u64(), dbuf.u64(), cols, 1, len, dir == GL_INVERSE,
-                           scratch ? dbuf.u64() + len : nullptr, stream);
+                              scratch ? dbuf.u64() + len : nullptr, stream);
     if (st == GL_OK)
       st = gl_cuda_status(cudaMemcpyAsync(data, dbuf.u64(), len * 8, cudaMemcpyDeviceToHost, stream));
   }
@@ -875,13 +916,15 @@ static int lde_device(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t co
   if (st != GL_OK) return st;
   // The forward pass reads only the first n rows of the zero-padded input: in
   // the four-step view j = n2*j1 + j2 that is j1 < n / n2, so n2 must divide n.
-  if (pm->kind == 2 && n % pm->n2 != 0) return GL_ERR_UNSUPPORTED_SIZE;
-  if (pm->kind == 3 && n % (pm->n2 * pm->n3) != 0) return GL_ERR_UNSUPPORTED_SIZE;
+  // Otherwise (and for Rader plans) the coset shift and the padding take a
+  // pass of their own before a plain transform.
+  const bool fused = pm->kind <= 1 || (pm->kind == 2 && n % pm->n2 == 0) ||
+                     (pm->kind == 3 && n % (pm->n2 * pm->n3) == 0);
   const uint64_t *clo = nullptr, *chi = nullptr;
   if ((st = coset_tables(shift % GL_P, n, &clo, &chi)) != GL_OK) return st;
   // Coefficients (n x cols) plus scratch for the larger of the two transforms.
   const uint64_t nc = n * cols, mc = m * cols;
-  const uint64_t scratch_words = std::max(pn->kind >= 2 ? nc : 0, pm->kind >= 2 ? mc : 0);
+  const uint64_t scratch_words = std::max(gl_plan_scratch_words(pn, cols, 1), gl_plan_scratch_words(pm, cols, 1));
   gl_tmp tmp;
   if ((st = tmp.alloc((nc + scratch_words) * sizeof(uint64_t), stream)) != GL_OK) return st;
   uint64_t *coef = tmp.u64(), *scr = tmp.u64() + nc;
@@ -891,15 +934,36 @@ static int lde_device(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t co
   } else if ((st = gl_enqueue_transform(pn, in, coef, cols, 1, nc, true, scr, stream)) != GL_OK) {
     return st;
   }
-  gl_load_opts lo;
-  lo.in_limit = (uint32_t)(pm->kind == 2 ? n / pm->n2 : pm->kind == 3 ? n / (pm->n2 * pm->n3) : n);
-  lo.itw_lo = clo;
-  lo.itw_hi = chi;
   if (pm->kind == 0) {  // m == 1: the value is the constant coefficient
     cudaError_t e = cudaMemcpyAsync(out, coef, nc * 8, cudaMemcpyDeviceToDevice, stream);
     return gl_cuda_status(e);
   }
+  if (!fused) {
+    if ((st = gl_coset_pad(coef, out, n, m, cols, clo, chi, stream)) != GL_OK) return st;
+    return gl_enqueue_transform(pm, out, out, cols, 1, mc, false, scr, stream);
+  }
+  gl_load_opts lo;
+  lo.in_limit = (uint32_t)(pm->kind == 2 ? n / pm->n2 : pm->kind == 3 ? n / (pm->n2 * pm->n3) : n);
+  lo.itw_lo = clo;
+  lo.itw_hi = chi;
   return gl_enqueue_transform(pm, coef, out, cols, 1, mc, false, scr, stream, &lo);
+}
+
+__global__ void gl_coset_pad_kernel(const uint64_t *coef, uint64_t *dst, uint64_t n, uint64_t m,
+                                    uint64_t cols, const uint64_t *g_lo, const uint64_t *g_hi) {
+  const uint64_t total = m * cols;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t j = i / cols;
+    dst[i] = j < n ? gl_mul(coef[i], gl_tw2(g_lo, g_hi, j)) : 0;
+  }
+}
+
+int gl_coset_pad(const uint64_t *coef, uint64_t *dst, uint64_t n, uint64_t m, uint64_t cols,
+                 const uint64_t *g_lo, const uint64_t *g_hi, cudaStream_t stream) {
+  const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((m * cols + 255) / 256, 152 * 32));
+  gl_coset_pad_kernel<<<blocks, 256, 0, stream>>>(coef, dst, n, m, cols, g_lo, g_hi);
+  return gl_cuda_status(cudaGetLastError());
 }
 
 extern "C" int gl_coset_lde(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t cols,

@@ -62,6 +62,7 @@ size_t max_shape_smem() {
 }
 
 int shape_index(const gl_kernel_entry *k, bool inv) {
+  if (!k) return -1;
   for (int i = 0; i < kNumShapes; i++)
     if (kShapes[i].r1 == k->r1 && kShapes[i].r2 == k->r2 && kShapes[i].r3 == k->r3)
       return 2 * i + (inv ? 1 : 0);
@@ -343,7 +344,7 @@ int run_buckets(const gl_poly *polys, uint64_t count, const std::vector<poly_pla
   // Group by (len, dir); order within a bucket = input order.
   std::map<std::pair<uint64_t, int>, std::vector<uint64_t>> buckets;
   for (uint64_t i = 0; i < count; i++) {
-    if (pp[i].pl->kind == 3) {  // three-pass sizes run as plain calls
+    if (pp[i].pl->kind >= 3) {  // three-pass and Rader sizes run as plain calls
       int st = run_per_call(&polys[i], 1, stream, false);
       if (st != GL_OK) return st;
     } else if (pp[i].pl->kind > 0) {

@@ -5,23 +5,33 @@
 
 #include "gl_internal.h"
 
-// Length-1 sequences have no transform pass to carry the product.
-__global__ void gl_pointwise_kernel(uint64_t *a, const uint64_t *b, uint64_t count, bool shared,
-                                    bool mont) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+// The pointwise product as a pass of its own: for length-1 sequences (no
+// transform pass to carry it) and Rader plans.  a[i] *= b[shared ? i % n : i].
+__global__ void gl_pointwise_kernel(uint64_t *a, const uint64_t *b, uint64_t total, uint64_t n,
+                                    bool shared, bool mont) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
        i += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t v = gl_mul(a[i], b[shared ? 0 : i]);
+    uint64_t v = gl_mul(a[i], b[shared ? i % n : i]);
     a[i] = mont ? gl_shl<128>(v) : v;  // 2^128 = 2^-64
   }
+}
+
+static int pointwise(uint64_t *a, const uint64_t *b, uint64_t total, uint64_t n, bool shared, bool mont,
+                     cudaStream_t stream) {
+  const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((total + 255) / 256, 152 * 16));
+  gl_pointwise_kernel<<<blocks, 256, 0, stream>>>(a, b, total, n, shared, mont);
+  return gl_cuda_status(cudaGetLastError());
 }
 
 static int convolve_device(gl_plan *pl, uint64_t *a, const uint64_t *b, uint64_t n,
                            uint64_t count, bool shared, bool mont, uint64_t *scratch,
                            cudaStream_t stream) {
-  if (pl->kind == 0) {
-    const unsigned blocks = (unsigned)std::min<uint64_t>((count + 255) / 256, 152 * 16);
-    gl_pointwise_kernel<<<blocks, 256, 0, stream>>>(a, b, count, shared, mont);
-    return gl_cuda_status(cudaGetLastError());
+  if (pl->kind == 0) return pointwise(a, b, count, 1, shared, mont, stream);
+  if (pl->kind == 4) {
+    int st = gl_enqueue_transform(pl, a, a, 1, count, n, false, scratch, stream);
+    if (st == GL_OK) st = pointwise(a, b, n * count, n, shared, mont, stream);
+    if (st == GL_OK) st = gl_enqueue_transform(pl, a, a, 1, count, n, true, scratch, stream);
+    return st;
   }
   gl_store_mul om;
   om.factors = b; om.shared = shared; om.mont = mont;
@@ -45,7 +55,7 @@ extern "C" int gl_convolve(uint64_t *a, const uint64_t *b_hat, uint64_t n, uint6
   const bool mont = repr == GL_REPR_MONTGOMERY;
   gl_init_mempool_once();
   const uint64_t len = n * count, blen = n * b_count;
-  const uint64_t need = pl->kind >= 2 ? len : 0;  // scratch words
+  const uint64_t need = gl_plan_scratch_words(pl, 1, count);  // scratch words
   if (mem == GL_MEM_DEVICE) {
     uint64_t *scratch = nullptr;
     if (need) {

@@ -60,14 +60,25 @@ struct gl_dev_tables {
   uint64_t *blk3[2] = {nullptr, nullptr};
   uint64_t *tw23_lo[2] = {nullptr, nullptr};
   uint64_t *tw23_hi[2] = {nullptr, nullptr};
+  // kind 4 only (gl_rader.cu): the transformed Rader kernel per direction,
+  // the index maps g^p and g^-p mod q, and the two-level table of omega_n
+  // (the inverse one scaled by 1/q).
+  uint64_t *rader_bhat[2] = {nullptr, nullptr};
+  uint32_t *rader_gpow = nullptr, *rader_gneg = nullptr;
+  uint64_t *rader_tw_lo[2] = {nullptr, nullptr};
+  uint64_t *rader_tw_hi[2] = {nullptr, nullptr};
   std::vector<void *> owned;
 };
 
 struct gl_plan {
   uint64_t size = 0;
-  int kind = 0;  // 0: no-op (size <= 1), 1: FULL, 2: COL+ROW, 3: COL+COL+ROW
+  int kind = 0;  // 0: no-op (size <= 1), 1: FULL, 2: COL+ROW, 3: COL+COL+ROW,
+                 // 4: Rader step over a prime factor q (257 or 65537), then size/q
   uint64_t n1 = 0, n2 = 0;  // kind 2: COL over n1, ROW over n2
   uint64_t n3 = 0;          // kind 3: COL over n1, COL over n2 (per k1), ROW over n3
+  uint64_t q = 0;           // kind 4: the prime factor; size = q * m
+  gl_plan *pq = nullptr;    // kind 4: plan of q - 1 (the cyclic convolution)
+  gl_plan *pm = nullptr;    // kind 4: plan of m = size / q (may itself be kind 4)
   const gl_kernel_entry *k[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};  // [stage][dir]
   std::string tree;
   std::mutex mu;
@@ -99,6 +110,22 @@ struct gl_store_mul {
   bool shared = false;
   bool mont = false;
 };
+
+// Device scratch (in words) that gl_enqueue_transform needs for B items of
+// C interleaved columns.
+uint64_t gl_plan_scratch_words(const gl_plan *pl, uint64_t C, uint64_t B);
+
+// Kind-4 plans (gl_rader.cu): the tables, and the transform (no load or store
+// options; items one after another, so the scratch is that of one item).
+int gl_rader_tables(gl_plan *pl, gl_dev_tables &t);
+int gl_rader_enqueue(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64_t C, uint64_t B,
+                     uint64_t bs, bool inv, uint64_t *scratch, cudaStream_t stream);
+uint64_t gl_rader_scratch_words(const gl_plan *pl, uint64_t C);
+
+// dst[j*cols + c] = j < n ? coef[j*cols + c] * g^j : 0 for j < m (the coset
+// shift and zero padding of an LDE as their own pass; gl_api.cu).
+int gl_coset_pad(const uint64_t *coef, uint64_t *dst, uint64_t n, uint64_t m, uint64_t cols,
+                 const uint64_t *g_lo, const uint64_t *g_hi, cudaStream_t stream);
 
 // Queue the transform of a strided batch on `stream`.  Element j of column c
 // of batch item b is at base[b*bs + j*C + c]; `src` and `dst` may be equal;

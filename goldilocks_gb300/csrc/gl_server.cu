@@ -82,14 +82,18 @@ uint64_t out_rows(const gl_request &r) { return r.op == GL_OP_LDE ? r.n * r.blow
 int footprint(const gl_request &r, uint64_t *bytes) {
   if (r.cols == 0 || (!r.in && r.n) || (!r.out && r.n)) return GL_ERR_INVALID;
   if (r.op != GL_OP_NTT && r.op != GL_OP_INTT && r.op != GL_OP_LDE) return GL_ERR_INVALID;
-  if (!gl_is_divisor(r.n)) return GL_ERR_UNSUPPORTED_SIZE;
+  gl_plan *pn = nullptr;
+  int st = gl_plan_create(r.n, &pn);
+  if (st != GL_OK) return st;
   if (r.op == GL_OP_LDE) {
     if (r.blowup == 0) return GL_ERR_INVALID;
-    if (!gl_is_divisor(r.n * (uint64_t)r.blowup)) return GL_ERR_UNSUPPORTED_SIZE;
-    // coefficients (n x cols) + scratch of the larger transform (blowup*n x cols)
-    *bytes = (r.n + r.n * (uint64_t)r.blowup) * r.cols * 8;
+    gl_plan *pm = nullptr;
+    if ((st = gl_plan_create(r.n * (uint64_t)r.blowup, &pm)) != GL_OK) return st;
+    // coefficients (n x cols) + scratch of the larger transform
+    *bytes = (r.n * r.cols + std::max(gl_plan_scratch_words(pn, r.cols, 1),
+                                      gl_plan_scratch_words(pm, r.cols, 1))) * 8;
   } else {
-    *bytes = r.n * r.cols * 8;  // scratch of a two- or three-pass transform
+    *bytes = gl_plan_scratch_words(pn, r.cols, 1) * 8;  // scratch of the transform
   }
   return GL_OK;
 }

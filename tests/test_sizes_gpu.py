@@ -1,10 +1,8 @@
-"""GPU parity over the size space: every transform length the plans support
-up to 2^16 (products of 2^k, 3, 5 and 17), larger mixed-radix lengths, and
-batched / column / LDE calls at such lengths, against the oracle.
-
-The reference plans any divisor of p - 1 (ntt/src/ntt/mod.rs:21-48 strategy
-choice); lengths that keep 257 or 65537 as a factor raise the unsupported-size
-error here."""
+"""GPU parity over the size space: every divisor of p - 1 up to 2^17 (the
+reference plans any divisor: ntt/src/ntt/mod.rs:48-78), larger mixed-radix
+lengths, and batched / column / LDE calls at such lengths, against the
+oracle.  Lengths with a factor 257 or 65537 take the Rader step; the others
+the compiled or run-time-radix pass kernels."""
 import numpy as np
 import pytest
 
@@ -21,9 +19,9 @@ def supported(gl, n):
         return False
 
 
-def test_every_supported_size_up_to_2p16(gl, oracle, cuda):
-    sizes = [n for n in gl.divisors() if 2 <= n <= 1 << 16 and n % 257 and n % 65537]
-    assert len(sizes) == 100  # 17 powers of two x {1, 3, 5, 15, 17, 51, 85, 255}, <= 2^16
+def test_every_divisor_up_to_2p17(gl, oracle, cuda):
+    sizes = [n for n in gl.divisors() if 2 <= n <= 1 << 17]
+    assert len(sizes) == 153  # 45 of them with a factor 257 or 65537
     for n in sizes:
         assert supported(gl, n), n
         x = rand_field(n * 3, seed=n)
