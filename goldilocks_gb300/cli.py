@@ -1,11 +1,16 @@
 """Command-line timing of single transforms, after the reference's bench binary
-(bench/src/main.rs:111-189: sweep sizes, print `size,duration,throughput`).
+(bench/src/main.rs:111-189: sweep the divisors up to 2^max_exponent -- the
+smooth ones, without the factors 17, 257, 65537, unless --all -- and print
+`size,duration,throughput`).
 
   python -m goldilocks_gb300.cli --sizes 16777216 --reps 3     # one size
-  python -m goldilocks_gb300.cli --max-exponent 24             # smooth divisors
+  python -m goldilocks_gb300.cli --max-exponent 24 --all       # every divisor
+  python -m goldilocks_gb300.cli --algo merkle --max-exponent 24
   python -m goldilocks_gb300.cli --sizes 1048576 --cols 256 --lde 4
 
-Inputs are device-resident; durations are CUDA-event medians (seconds).
+Algorithms (the reference's `--algo`): ntt, inverse, merkle (the K12 tree of
+the size*8 bytes of field elements).  Inputs are device-resident; durations
+are CUDA-event medians (seconds).
 """
 import argparse
 import statistics
@@ -19,10 +24,13 @@ def main(argv=None):
     ap.add_argument("--all", action="store_true", help="all divisors, not only smooth ones")
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=2)
-    ap.add_argument("--inverse", action="store_true")
+    ap.add_argument("--inverse", action="store_true", help="same as --algo inverse")
+    ap.add_argument("--algo", choices=["ntt", "inverse", "merkle"], default="ntt")
     ap.add_argument("--cols", type=int, default=1, help="transform the columns of a rows x cols matrix")
     ap.add_argument("--lde", type=int, default=0, help="coset LDE with this blowup (shift 7)")
     args = ap.parse_args(argv)
+    if args.inverse:
+        args.algo = "inverse"
 
     import numpy as np
     import torch
@@ -34,9 +42,9 @@ def main(argv=None):
     if args.sizes:
         sizes = [int(s) for s in args.sizes.split(",")]
     else:
-        smooth = 64424509440  # 2^32 * 3 * 5: divisors without 17, 257, 65537
+        smooth = 64424509440  # 2^32 * 3 * 5 (divisors.rs:7): no factor 17, 257, 65537
         sizes = [d for d in gl.divisors() if 2 <= d <= (1 << args.max_exponent)
-                 and (args.all or smooth % d == 0 or d % 17 == 0 and smooth * 17 % d == 0)]
+                 and (args.all or smooth % d == 0)]
     stream = torch.cuda.current_stream()
     print("size,cols,duration,throughput")
     for n in sizes:
@@ -46,17 +54,25 @@ def main(argv=None):
         if args.lde:
             out = torch.empty(n * args.cols * args.lde, dtype=torch.int64, device="cuda")
 
+        tree = None
+        if args.algo == "merkle":
+            tree = torch.empty(max(lib.gl_merkle_tree_bytes(n * args.cols * 8), 1), dtype=torch.uint8,
+                               device="cuda")
+
         def run():
-            if args.lde:
+            if tree is not None:
+                rc = lib.gl_merkle_tree(d.data_ptr(), n * args.cols * 8, tree.data_ptr(), tree.numel(),
+                                        L.GL_MEM_DEVICE, stream.cuda_stream)
+            elif args.lde:
                 rc = lib.gl_coset_lde(d.data_ptr(), out.data_ptr(), n, args.cols, args.lde, 7,
                                       L.GL_MEM_DEVICE, stream.cuda_stream)
             elif args.cols > 1:
                 rc = lib.gl_ntt_columns(d.data_ptr(), n, args.cols,
-                                        L.GL_INVERSE if args.inverse else L.GL_FORWARD,
+                                        L.GL_INVERSE if args.algo == "inverse" else L.GL_FORWARD,
                                         L.GL_MEM_DEVICE, stream.cuda_stream)
             else:
                 pl = gl.strategy(n)
-                (pl.intt if args.inverse else pl.ntt)(d)
+                (pl.intt if args.algo == "inverse" else pl.ntt)(d)
                 rc = 0
             if rc:
                 raise gl.GoldilocksError(rc, "cli")
