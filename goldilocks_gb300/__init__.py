@@ -2,7 +2,7 @@
 recmo/goldilocks' `goldilocks-ntt` crate behind a C ABI (include/goldilocks_gpu.h).
 """
 from .ntt import (MODULUS, GoldilocksError, Plan, clear_cache, convolve, divisors, fill_uniform,
-                  intt, is_divisor, next, ntt, split, strategy)
+                  host_pipeline, intt, is_divisor, next, ntt, split, strategy)
 
 __all__ = ["MODULUS", "GoldilocksError", "Plan", "clear_cache", "convolve", "divisors", "fill_uniform",
-           "intt", "is_divisor", "next", "ntt", "split", "strategy"]
+           "host_pipeline", "intt", "is_divisor", "next", "ntt", "split", "strategy"]

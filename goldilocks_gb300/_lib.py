@@ -36,6 +36,7 @@ SIGNATURES = [
     ("gl_ntt_columns", _int, [_vp, _u64, _u64, _int, _int, _vp]),
     ("gl_coset_lde", _int, [_vp, _vp, _u64, _u64, _u32, _u64, _int, _vp]),
     ("gl_convolve", _int, [_vp, _vp, _u64, _u64, _u64, _int, _int, _vp]),
+    ("gl_host_pipeline", _int, [_vp, _u64, _u32]),
     ("gl_k12_next_layer_size", _u64, [_u64]),
     ("gl_merkle_tree_bytes", _u64, [_u64]),
     ("gl_k12_process_layer", _int, [_vp, _u64, _vp, _int, _vp]),
@@ -71,6 +72,13 @@ GL_BATCH_AUTO, GL_BATCH_PERSISTENT, GL_BATCH_BUCKETS, GL_BATCH_PER_CALL = 0, 1, 
 GL_OP_NTT, GL_OP_INTT, GL_OP_LDE = 0, 1, 2
 
 GL_REPR_CANONICAL, GL_REPR_MONTGOMERY = 0, 1
+
+GL_HOST_JOB_MAX_OPS = 4
+
+
+class HostJob(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("len", ctypes.c_uint64), ("count", ctypes.c_uint64),
+                ("nops", ctypes.c_uint32), ("dirs", ctypes.c_int32 * GL_HOST_JOB_MAX_OPS)]
 
 
 class Request(ctypes.Structure):

@@ -756,6 +756,37 @@ void gl_init_mempool_once() {
   });
 }
 
+// Device address of host memory [p, p + bytes) that kernels can read and
+// write in place: page-locked memory mapped into the device address space
+// (cudaHostAlloc / cudaMallocHost / cudaHostRegister under unified
+// addressing; on Grace-Blackwell the GPU reaches it over NVLink-C2C).  Both
+// ends of the range must be such memory, else nullptr and the caller stages
+// through device memory.  GOLDILOCKS_HOST_STAGING=1 forces staging.
+void *gl_host_device_view(const void *p, uint64_t bytes) {
+  static const bool staging = [] {
+    const char *v = getenv("GOLDILOCKS_HOST_STAGING");
+    return v && v[0] == '1';
+  }();
+  if (staging || !p || bytes == 0) return nullptr;
+  cudaPointerAttributes a0, a1;
+  const char *last = (const char *)p + bytes - 1;
+  if (cudaPointerGetAttributes(&a0, p) != cudaSuccess || cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
+    cudaGetLastError();  // clear the error of an unknown pointer
+    return nullptr;
+  }
+  if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer ||
+      !a1.devicePointer)
+    return nullptr;
+  if ((const char *)a1.devicePointer - (const char *)a0.devicePointer != (ptrdiff_t)(bytes - 1)) return nullptr;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || a0.device != dev) {
+    // mapped for another device's context; with unified addressing pinned
+    // memory is portable, so the same address serves every device
+    if (a0.devicePointer != p) return nullptr;
+  }
+  return a0.devicePointer;
+}
+
 static int execute(gl_plan *pl, uint64_t *data, uint64_t len, int dir, int mem, void *ws,
                    uint64_t ws_bytes, cudaStream_t stream) {
   if (!pl || (!data && len)) return GL_ERR_INVALID;
@@ -781,6 +812,19 @@ static int execute(gl_plan *pl, uint64_t *data, uint64_t len, int dir, int mem, 
     st = run_device(pl, data, count, inv, scratch, stream);
     if (own) cudaFreeAsync(scratch, stream);
     return st;
+  }
+  // Host memory the GPU addresses directly: the first pass reads it and the
+  // last pass writes it; only the scratch lives in device memory.
+  if (uint64_t *hv = (uint64_t *)gl_host_device_view(data, len * sizeof(uint64_t))) {
+    uint64_t *scratch = nullptr;
+    if (need) {
+      cudaError_t e = cudaMallocAsync((void **)&scratch, need, stream);
+      if (e != cudaSuccess) return gl_cuda_status(e);
+    }
+    st = run_device(pl, hv, count, inv, scratch, stream);
+    if (scratch) cudaFreeAsync(scratch, stream);
+    cudaError_t e = cudaStreamSynchronize(stream);
+    return st != GL_OK ? st : gl_cuda_status(e);
   }
   // Host memory: stage through the device and return when the result is back.
   uint64_t *dbuf = nullptr;

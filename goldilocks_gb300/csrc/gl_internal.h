@@ -111,6 +111,10 @@ struct gl_store_mul {
   bool mont = false;
 };
 
+// Device address of page-locked, device-mapped host memory [p, p + bytes), or
+// nullptr (then host data is staged through device memory).  (gl_api.cu)
+void *gl_host_device_view(const void *p, uint64_t bytes);
+
 // Device scratch (in words) that gl_enqueue_transform needs for B items of
 // C interleaved columns.
 uint64_t gl_plan_scratch_words(const gl_plan *pl, uint64_t C, uint64_t B);

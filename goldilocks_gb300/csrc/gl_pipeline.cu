@@ -1,0 +1,134 @@
+// Transforms of host buffers with the copies overlapped (no counterpart in the
+// reference, whose transforms run where the data lives).
+//
+// Each job is one round trip: its buffer is copied to the device once, gets
+// every transform of its op list there, and is copied back once.  Three
+// streams per device -- copy-in, compute, copy-out -- with a ring of `depth`
+// device slots, so job i+1 is copied in while job i computes and job i-1 is
+// copied out.  The host-device link carries both directions at once (on
+// GB300 about 340 GB/s together against about 200 GB/s one way), so the
+// overlap nearly halves the copy time of a plain call per transform.
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "gl_internal.h"
+
+namespace {
+
+struct pipe_streams {
+  cudaStream_t in = nullptr, comp = nullptr, out = nullptr;
+  std::mutex mu;  // one pipeline per device at a time
+};
+
+std::mutex g_pipe_mu;
+std::map<int, pipe_streams *> g_pipes;
+
+int streams_for_device(pipe_streams **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return gl_cuda_status(e);
+  std::lock_guard<std::mutex> lk(g_pipe_mu);
+  auto it = g_pipes.find(dev);
+  if (it == g_pipes.end()) {
+    auto *p = new pipe_streams();
+    if ((e = cudaStreamCreateWithFlags(&p->in, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&p->comp, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&p->out, cudaStreamNonBlocking)) != cudaSuccess)
+      return gl_cuda_status(e);
+    it = g_pipes.emplace(dev, p).first;
+  }
+  *out = it->second;
+  return GL_OK;
+}
+
+struct events {
+  std::vector<cudaEvent_t> ev;
+  ~events() { for (auto e : ev) cudaEventDestroy(e); }
+  int make(size_t n) {
+    ev.resize(n, nullptr);
+    for (auto &e : ev)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return GL_ERR_CUDA;
+    return GL_OK;
+  }
+};
+
+}  // namespace
+
+extern "C" int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_t depth) {
+  if (njobs == 0) return GL_OK;
+  if (!jobs) return GL_ERR_INVALID;
+  if (depth == 0) depth = 3;
+  depth = (uint32_t)std::min<uint64_t>(depth, njobs);
+  // Plans and sizes first: nothing is queued for an invalid batch.
+  std::vector<gl_plan *> plans(njobs, nullptr);
+  uint64_t slot_words = 0, scratch_words = 0;
+  for (uint64_t i = 0; i < njobs; i++) {
+    const gl_host_job &j = jobs[i];
+    if (j.nops > GL_HOST_JOB_MAX_OPS || (!j.data && j.len && j.count)) return GL_ERR_INVALID;
+    for (uint32_t k = 0; k < j.nops; k++)
+      if (j.dirs[k] != GL_FORWARD && j.dirs[k] != GL_INVERSE) return GL_ERR_INVALID;
+    int st = gl_plan_create(j.len, &plans[i]);
+    if (st != GL_OK) return st;
+    slot_words = std::max(slot_words, j.len * j.count);
+    for (uint32_t k = 0; k < j.nops; k++)
+      if (!(j.dirs[k] == GL_INVERSE && j.len <= 1))
+        scratch_words = std::max(scratch_words, gl_plan_scratch_words(plans[i], 1, j.count));
+  }
+  pipe_streams *ps = nullptr;
+  int st = streams_for_device(&ps);
+  if (st != GL_OK) return st;
+  std::lock_guard<std::mutex> lk(ps->mu);
+  gl_init_mempool_once();
+  uint64_t *block = nullptr;
+  const uint64_t words = depth * slot_words + scratch_words;
+  cudaError_t e = cudaMallocAsync((void **)&block, std::max<uint64_t>(words, 1) * 8, ps->comp);
+  if (e != cudaSuccess) return gl_cuda_status(e);
+  events ready, done, freed, alloc;
+  if ((st = ready.make(njobs)) != GL_OK || (st = done.make(njobs)) != GL_OK ||
+      (st = freed.make(njobs)) != GL_OK || (st = alloc.make(1)) != GL_OK) {
+    cudaFreeAsync(block, ps->comp);
+    return st;
+  }
+  cudaEventRecord(alloc.ev[0], ps->comp);  // the block exists for the copy streams
+  cudaStreamWaitEvent(ps->in, alloc.ev[0], 0);
+  uint64_t *scratch = block + depth * slot_words;
+  for (uint64_t i = 0; i < njobs && st == GL_OK; i++) {
+    const gl_host_job &j = jobs[i];
+    uint64_t *buf = block + (i % depth) * slot_words;
+    const uint64_t words_i = j.len * j.count;
+    if (i >= depth) cudaStreamWaitEvent(ps->in, freed.ev[i - depth], 0);  // slot copied out
+    if (words_i)
+      e = cudaMemcpyAsync(buf, j.data, words_i * 8, cudaMemcpyHostToDevice, ps->in);
+    if (e != cudaSuccess) { st = gl_cuda_status(e); break; }
+    cudaEventRecord(ready.ev[i], ps->in);
+    cudaStreamWaitEvent(ps->comp, ready.ev[i], 0);
+    for (uint32_t k = 0; k < j.nops && st == GL_OK && words_i; k++) {
+      const bool inv = j.dirs[k] == GL_INVERSE;
+      if (inv && j.len <= 1) continue;  // ntt/src/ntt/mod.rs:105-107
+      st = gl_enqueue_transform(plans[i], buf, buf, 1, j.count, j.len, inv, scratch, ps->comp);
+    }
+    cudaEventRecord(done.ev[i], ps->comp);
+    cudaStreamWaitEvent(ps->out, done.ev[i], 0);
+    if (words_i && st == GL_OK)
+      e = cudaMemcpyAsync(j.data, buf, words_i * 8, cudaMemcpyDeviceToHost, ps->out);
+    if (e != cudaSuccess) st = gl_cuda_status(e);
+    cudaEventRecord(freed.ev[i], ps->out);
+  }
+  // The block is freed on the compute stream once every copy-out is done.
+  cudaEvent_t last = nullptr;
+  if (cudaEventCreateWithFlags(&last, cudaEventDisableTiming) == cudaSuccess) {
+    cudaEventRecord(last, ps->out);
+    cudaStreamWaitEvent(ps->comp, last, 0);
+  }
+  cudaFreeAsync(block, ps->comp);
+  cudaError_t e1 = cudaStreamSynchronize(ps->in);
+  cudaError_t e2 = cudaStreamSynchronize(ps->out);
+  cudaError_t e3 = cudaStreamSynchronize(ps->comp);
+  if (last) cudaEventDestroy(last);
+  if (st != GL_OK) return st;
+  if (e1 != cudaSuccess) return gl_cuda_status(e1);
+  if (e2 != cudaSuccess) return gl_cuda_status(e2);
+  return gl_cuda_status(e3);
+}

@@ -155,6 +155,31 @@ def convolve(a, b_hat, size=None, montgomery=True):
     return a
 
 
+def host_pipeline(jobs, depth=0):
+    """Transform host buffers with the copies overlapped: `jobs` is a list of
+    (numpy uint64 array, size, [directions...]) -- each array holds
+    len/size transforms and gets the listed transforms (ntt/intt by
+    "fwd"/"inv") in order, in place, with one copy in and one copy out."""
+    arr = (L.HostJob * max(len(jobs), 1))()
+    keep = []
+    for i, (a, size, dirs) in enumerate(jobs):
+        if not isinstance(a, np.ndarray) or a.dtype != np.uint64 or not a.flags.c_contiguous:
+            raise TypeError("jobs need C-contiguous numpy uint64 arrays")
+        if size <= 0 or a.size % size:
+            raise ValueError("array length is not a multiple of the transform size")
+        if len(dirs) > L.GL_HOST_JOB_MAX_OPS:
+            raise ValueError("at most %d transforms per job" % L.GL_HOST_JOB_MAX_OPS)
+        keep.append(a)
+        arr[i].data = a.ctypes.data if a.size else None
+        arr[i].len, arr[i].count, arr[i].nops = size, a.size // size, len(dirs)
+        for k, d in enumerate(dirs):
+            arr[i].dirs[k] = L.GL_INVERSE if d in ("inv", L.GL_INVERSE) else L.GL_FORWARD
+    st = L.load().gl_host_pipeline(ctypes.addressof(arr), len(jobs), depth)
+    bad = [s for _, s, _ in jobs if not is_divisor(s)]
+    _check(st, "host_pipeline", size=bad[0] if bad else None)
+    return [a for a, _, _ in jobs]
+
+
 def clear_cache():
     L.load().gl_clear_cache()
 

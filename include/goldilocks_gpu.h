@@ -137,6 +137,30 @@ enum { GL_REPR_CANONICAL = 0, GL_REPR_MONTGOMERY = 1 };
 int gl_convolve(uint64_t *a, const uint64_t *b_hat, uint64_t n, uint64_t count, uint64_t b_count,
                 int repr, int mem, void *stream);
 
+/* ---- host buffers with overlapped copies (no counterpart in the reference) ---- */
+
+#define GL_HOST_JOB_MAX_OPS 4
+
+/* One round trip of a host buffer: `count` transforms of length `len` back to
+ * back in `data`, each getting the transforms dirs[0..nops) in order (for
+ * example GL_FORWARD then GL_INVERSE), in place. */
+typedef struct {
+  uint64_t *data;
+  uint64_t len;
+  uint64_t count;
+  uint32_t nops;
+  int32_t dirs[GL_HOST_JOB_MAX_OPS];
+} gl_host_job;
+
+/* Run the jobs with the host-device copies overlapped: each buffer is copied
+ * to the device once and back once, and job i+1 is copied in while job i
+ * computes and job i-1 is copied out (copy-in, compute and copy-out streams
+ * of the library; `depth` device slots, 0 = 3).  Synchronous: returns when
+ * every buffer holds its result.  Page-locked host memory overlaps; pageable
+ * memory works but its copies do not overlap.  The results equal those of
+ * gl_plan_execute per transform. */
+int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_t depth);
+
 /* ---- K12 Merkle layers and proof of work (pcs/src/k12, pcs/src/pow.rs) ----
  *
  * Byte-oriented; `mem` applies to every data buffer of a call (the 32-byte

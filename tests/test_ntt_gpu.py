@@ -38,6 +38,21 @@ def test_host_memory_path(gl, oracle, n):
     assert np.array_equal(y, x)
 
 
+@pytest.mark.parametrize("n,count", [(4096, 3), (1 << 16, 2), (1 << 22, 1), (1 << 25, 1), (257 * 16, 3),
+                                     (3 << 20, 1)])
+def test_pinned_host_memory_in_place(gl, oracle, cuda, n, count):
+    """Page-locked host buffers are read and written by the kernels in place
+    (no staging copies); pageable ones (numpy) are staged."""
+    t = cuda.empty(n * count, dtype=cuda.int64, pin_memory=True)
+    h = t.numpy().view(np.uint64)
+    x = gl.fill_uniform(n * count, seed=n + count)
+    h[:] = x
+    gl.strategy(n).ntt(h)
+    assert np.array_equal(h, oracle.ntt(x, size=n))
+    gl.strategy(n).intt(h)
+    assert np.array_equal(h, x)
+
+
 @pytest.mark.parametrize("n,count", [(8, 1000), (64, 333), (1024, 37), (4096, 9), (1 << 14, 5)])
 def test_batched_plan(gl, oracle, cuda, n, count):
     x = rand_field(n * count, seed=count)

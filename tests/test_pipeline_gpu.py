@@ -1,0 +1,42 @@
+"""GPU: gl_host_pipeline (host buffers, one round trip each, copies
+overlapped) gives the same words as the per-call transforms."""
+import numpy as np
+import pytest
+
+from conftest import rand_field
+
+pytestmark = pytest.mark.gpu
+
+
+def pinned(cuda, x):
+    t = cuda.empty(x.size, dtype=cuda.int64, pin_memory=True)
+    h = t.numpy().view(np.uint64)
+    h[:] = x
+    return h
+
+
+@pytest.mark.parametrize("depth", [0, 1, 2, 5])
+def test_pipeline_matches_oracle(gl, oracle, cuda, depth):
+    specs = [(1 << 20, 1, ("fwd",)), (4096, 7, ("fwd", "inv")), (1 << 16, 2, ("inv",)),
+             (257 * 16, 3, ("fwd",)), (16711680, 1, ("fwd", "inv", "fwd")), (3 << 10, 5, ("inv", "fwd"))]
+    xs, jobs = [], []
+    for i, (n, count, dirs) in enumerate(specs):
+        x = rand_field(n * count, seed=i + 10 * depth)
+        xs.append(x)
+        h = pinned(cuda, x) if i % 2 == 0 else x.copy()   # page-locked and pageable buffers
+        jobs.append((h, n, dirs))
+    gl.host_pipeline(jobs, depth=depth)
+    for (h, n, dirs), x in zip(jobs, xs):
+        want = x
+        for d in dirs:
+            want = (oracle.ntt if d == "fwd" else oracle.intt)(want, size=n)
+        assert np.array_equal(h, want), (n, dirs)
+
+
+def test_pipeline_errors(gl, cuda):
+    x = rand_field(16, seed=1)
+    with pytest.raises(ValueError, match="is not a supported NTT size"):
+        gl.host_pipeline([(x[:7].copy(), 7, ("fwd",))])
+    with pytest.raises(ValueError, match="at most"):
+        gl.host_pipeline([(x, 16, ("fwd",) * 5)])
+    gl.host_pipeline([])
