@@ -170,8 +170,21 @@ static const gl_kernel_entry *generic_entry(uint64_t m, bool inv) {
   return &cache.emplace(key, e).first->second;
 }
 
+// GOLDILOCKS_PASS_LANES=4 keeps the four-lane kernels for every pass size.
+static bool use_two_lane_passes() {
+  static const bool on = [] {
+    const char *v = getenv("GOLDILOCKS_PASS_LANES");
+    return !(v && v[0] == '4');
+  }();
+  return on;
+}
+
 const gl_kernel_entry *gl_find_kernel(uint64_t m, bool full, bool inv) {
   size_t cnt = 0;
+  if (!full && use_two_lane_passes()) {
+    const gl_kernel_entry *e = inv ? gl_kernels_pass2_inv(&cnt) : gl_kernels_pass2_fwd(&cnt);
+    if (const gl_kernel_entry *k = find_in(e, cnt, m)) return k;
+  }
   if (!full && use_wide_kernels()) {
     const gl_kernel_entry *e = inv ? gl_kernels_wide_inv(&cnt) : gl_kernels_wide_fwd(&cnt);
     if (const gl_kernel_entry *k = find_in(e, cnt, m)) return k;
@@ -638,7 +651,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
         a.flags |= GL_PF_IN_TWIDDLE;
         a.itw_lo = lo->itw_lo; a.itw_hi = lo->itw_hi; a.itw_jmul = n23;
       }
-      const uint64_t ta = (n23 * C + GL_PASS_LANES - 1) / GL_PASS_LANES;
+      const uint64_t ta = gl_tiles(n23 * C, ka);
       if (ta > 0x7fffffffull) return GL_ERR_INVALID;
       gl_launch(ka, 1, a, dim3((unsigned)ta), n * C, stream);
       gl_pass_args bb = base_args();
@@ -650,7 +663,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       bb.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
       bb.tw_m = bb.tw_r2 = t->blk[1][d]; bb.tw_lo = t->tw23_lo[d]; bb.tw_hi = t->tw23_hi[d];
       bb.tw_lane_div = (uint32_t)C;
-      gl_launch(kb, 1, bb, dim3((unsigned)((n3 * C + GL_PASS_LANES - 1) / GL_PASS_LANES), (unsigned)n1),
+      gl_launch(kb, 1, bb, dim3((unsigned)gl_tiles(n3 * C, kb), (unsigned)n1),
                 n * C, stream);
       gl_pass_args c = base_args();
       c.in_limit = 0xffffffffu;
@@ -667,7 +680,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
           c.mul = om->factors + b * mul_item;
           c.mul_ls = c.out_ls; c.mul_bs = c.out_bs;
         }
-        gl_launch(kcr, 2, c, dim3((unsigned)(n2 / GL_PASS_LANES), (unsigned)n1), n, stream);
+        gl_launch(kcr, 2, c, dim3((unsigned)gl_tiles(n2, kcr), (unsigned)n1), n, stream);
       } else {
         c.in_ls = 1; c.in_is = (int64_t)C;                        // lanes: columns
         c.out_ls = 1; c.out_is = (int64_t)(n1 * n2 * C);
@@ -675,7 +688,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
         c.in_bs2 = (int64_t)(n23 * C); c.out_bs2 = (int64_t)C;          // grid.z: k1
         c.flags |= GL_PF_LOAD_LANE_FAST;
         c.lanes = (uint32_t)C;
-        gl_launch(kcr, 2, c, dim3((unsigned)((C + GL_PASS_LANES - 1) / GL_PASS_LANES), (unsigned)n2,
+        gl_launch(kcr, 2, c, dim3((unsigned)gl_tiles(C, kcr), (unsigned)n2,
                                   (unsigned)n1), n * C, stream);
       }
     }
@@ -705,8 +718,8 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       a.itw_lo = lo->itw_lo; a.itw_hi = lo->itw_hi; a.itw_jmul = n2;
     }
     const uint64_t lanes1 = n2 * C;
-    if ((lanes1 + GL_PASS_LANES - 1) / GL_PASS_LANES > 0x7fffffffull) return GL_ERR_INVALID;
-    gl_launch(kc, 1, a, dim3((unsigned)((lanes1 + GL_PASS_LANES - 1) / GL_PASS_LANES), (unsigned)cb),
+    if (gl_tiles(lanes1, kc) > 0x7fffffffull) return GL_ERR_INVALID;
+    gl_launch(kc, 1, a, dim3((unsigned)gl_tiles(lanes1, kc), (unsigned)cb),
            cb * n * C, stream);
     // ROW: n2-point transforms along j2 for every (k1, c); transposed store.
     gl_pass_args b = base_args();
@@ -723,7 +736,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
         b.mul = om->factors + off * mul_item;
         b.mul_ls = 1; b.mul_bs = mul_item;
       }
-      gl_launch(kr, 2, b, dim3((unsigned)(n1 / GL_PASS_LANES), (unsigned)cb), cb * n, stream);
+      gl_launch(kr, 2, b, dim3((unsigned)gl_tiles(n1, kr), (unsigned)cb), cb * n, stream);
     } else {
       b.in = scratch + off * n * C; b.out = dst + off * bs;
       b.in_ls = 1; b.in_is = (int64_t)C; b.out_ls = 1; b.out_is = (int64_t)(n1 * C);
@@ -731,7 +744,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       b.in_bs2 = (int64_t)(n * C); b.out_bs2 = (int64_t)bs;      // grid.z: batch
       b.flags |= GL_PF_LOAD_LANE_FAST;
       b.lanes = (uint32_t)C;
-      gl_launch(kr, 2, b, dim3((unsigned)((C + GL_PASS_LANES - 1) / GL_PASS_LANES), (unsigned)n1,
+      gl_launch(kr, 2, b, dim3((unsigned)gl_tiles(C, kr), (unsigned)n1,
                             (unsigned)cb), cb * n * C, stream);
     }
   }

@@ -403,12 +403,12 @@ int run_buckets(const gl_poly *polys, uint64_t count, const std::vector<poly_pla
         col.flags |= GL_PF_PTR_TABLE;
         col.in_ptrs = (const uint64_t *const *)(dt + j);
         col.out_ptrs = (uint64_t *const *)(dt + base_sc + j);
-        gl_launch(pl->k[0][d], 1, col, dim3((unsigned)(pl->n2 / GL_PASS_LANES), (unsigned)(j1 - j)),
+        gl_launch(pl->k[0][d], 1, col, dim3((unsigned)gl_tiles(pl->n2, pl->k[0][d]), (unsigned)(j1 - j)),
                   pl->size * (j1 - j), cap);
         row.flags |= GL_PF_PTR_TABLE;
         row.in_ptrs = (const uint64_t *const *)(dt + base_sc + j);
         row.out_ptrs = (uint64_t *const *)(dt + j);
-        gl_launch(pl->k[1][d], 2, row, dim3((unsigned)(pl->n1 / GL_PASS_LANES), (unsigned)(j1 - j)),
+        gl_launch(pl->k[1][d], 2, row, dim3((unsigned)gl_tiles(pl->n1, pl->k[1][d]), (unsigned)(j1 - j)),
                   pl->size * (j1 - j), cap);
       }
       j = j1;

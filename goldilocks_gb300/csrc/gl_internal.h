@@ -33,6 +33,9 @@ const gl_kernel_entry *gl_kernels_full_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_full_inv(size_t *count);
 const gl_kernel_entry *gl_kernels_pass_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_pass_inv(size_t *count);
+// Passes up to 2048 points with two lanes per CTA and four CTAs per SM.
+const gl_kernel_entry *gl_kernels_pass2_fwd(size_t *count);
+const gl_kernel_entry *gl_kernels_pass2_inv(size_t *count);
 // Two-round kernels with up to 64 elements per thread (an alternative the
 // autotuner may choose).
 const gl_kernel_entry *gl_kernels_wide_fwd(size_t *count);
@@ -43,10 +46,13 @@ void gl_launch_generic_fwd(const gl_pass_args &args, dim3 grid, cudaStream_t str
 void gl_launch_generic_inv(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
 #include "gl_generic.cuh"
 
+// CTAs that cover `lanes` lanes with kernel k.
+inline uint64_t gl_tiles(uint64_t lanes, const gl_kernel_entry *k) { return (lanes + k->lanes - 1) / k->lanes; }
+
 // Launch-time check: the kernel entry for (m, full, inv), or nullptr.
 const gl_kernel_entry *gl_find_kernel(uint64_t m, bool full, bool inv);
 
-#define GL_PASS_LANES 4
+#define GL_PASS_LANES 4  // pass sizes are multiples of it; every pass kernel's lanes divide it
 #define GL_TW_SPLIT 4096  // two-level pass twiddle: e = hi*4096 + lo
 
 // Device-resident twiddle tables of one plan on one device.

@@ -12,5 +12,5 @@ static void gl_launch_generic(const gl_pass_args &args, dim3 grid, cudaStream_t 
   gl_generic_kernel<INV><<<grid, GL_GEN_NT, smem, stream>>>(args);
 }
 
-// Pass launches size their grids by GL_PASS_LANES for every kernel.
-static_assert(GL_GEN_LANES == GL_PASS_LANES, "run-time-radix kernel lane count");
+// Pass sizes are multiples of GL_PASS_LANES; the kernel's lanes must divide it.
+static_assert(GL_PASS_LANES % GL_GEN_LANES == 0, "run-time-radix kernel lane count");

@@ -12,10 +12,10 @@ static void gl_launch_pass(const gl_pass_args &args, dim3 grid, cudaStream_t str
   kern<<<grid, LANES * MB, smem, stream>>>(args);
 }
 
-template <int R1, int R2, int R3, int LANES, int NT, bool INV>
+template <int R1, int R2, int R3, int LANES, int NT, bool INV, int MINB = 1>
 static void gl_launch_pass3(const gl_pass_args &args, dim3 grid, cudaStream_t stream) {
   constexpr size_t smem = gl_p3_smem_bytes<R1, R2, R3, LANES>();
-  auto kern = gl_pass3_kernel<R1, R2, R3, LANES, NT, INV>;
+  auto kern = gl_pass3_kernel<R1, R2, R3, LANES, NT, INV, MINB>;
   if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   kern<<<grid, NT, smem, stream>>>(args);
 }
@@ -26,3 +26,9 @@ static void gl_launch_pass3(const gl_pass_args &args, dim3 grid, cudaStream_t st
 #define GL_ENTRY3(R1, R2, R3, LANES, NT, INV)                                                 \
   {R1 * R2 * R3, R1, R2, R3, LANES, INV, gl_p3_smem_bytes<R1, R2, R3, LANES>(), NT,          \
    gl_launch_pass3<R1, R2, R3, LANES, NT, INV>}
+
+// MINB CTAs resident per SM (registers capped to fit), so that one CTA's
+// loads overlap another's arithmetic.
+#define GL_ENTRY3M(R1, R2, R3, LANES, NT, MINB, INV)                                          \
+  {R1 * R2 * R3, R1, R2, R3, LANES, INV, gl_p3_smem_bytes<R1, R2, R3, LANES>(), NT,          \
+   gl_launch_pass3<R1, R2, R3, LANES, NT, INV, MINB>}

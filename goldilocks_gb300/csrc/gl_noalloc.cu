@@ -116,7 +116,7 @@ extern "C" int gl_ntt_noalloc(uint64_t *data, uint64_t len, int dir, void *strea
   a.tw_m = a.tw_r2 = tab + GL_NOALLOC_T1;
   a.tw_lo = tab + GL_NOALLOC_TLO;
   a.tw_hi = tab + GL_NOALLOC_THI;
-  kc->launch(a, dim3((unsigned)(n2 / GL_PASS_LANES)), stream);
+  kc->launch(a, dim3((unsigned)gl_tiles(n2, kc)), stream);
 
   gl_pass_args b{};  // row pass: scratch -> data at the transposed position
   b.in = p.scratch; b.out = data;
@@ -126,7 +126,7 @@ extern "C" int gl_ntt_noalloc(uint64_t *data, uint64_t len, int dir, void *strea
   b.in_limit = 0xffffffffu;
   b.tw_lane_div = 1;
   b.tw_m = b.tw_r2 = tab + GL_NOALLOC_T2;
-  kr->launch(b, dim3((unsigned)(n1 / GL_PASS_LANES)), stream);
+  kr->launch(b, dim3((unsigned)gl_tiles(n1, kr)), stream);
 
   return cudaGetLastError() == cudaSuccess ? GL_OK : GL_ERR_CUDA;
 }

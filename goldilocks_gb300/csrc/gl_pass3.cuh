@@ -196,8 +196,8 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
   }
 }
 
-template <int R1, int R2, int R3, int LANES, int NT, bool INV>
-__global__ void __launch_bounds__(NT) gl_pass3_kernel(const gl_pass_args a) {
+template <int R1, int R2, int R3, int LANES, int NT, bool INV, int MINB = 1>
+__global__ void __launch_bounds__(NT, MINB) gl_pass3_kernel(const gl_pass_args a) {
   extern __shared__ uint64_t sm[];
   gl_block3<R1, R2, R3, LANES, NT, INV>(a, blockIdx.x, blockIdx.y, blockIdx.z, sm);
 }
