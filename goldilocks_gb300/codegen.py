@@ -10,7 +10,8 @@ device code in single-assignment form for register-resident data:
 * `gl_dft<R, INV>(uint64_t *x)` transforms R values held in registers, natural
   order in and out, with omega_R = 2717^((p-1)/R) (INV: omega_R^-1).
 * twiddles of order dividing 192 become `gl_shl<k>` (omega_192 = 2); other
-  twiddles are `gl_mul` by a literal.
+  twiddles and the Rader constants are `gl_mont_mul` by the literal's
+  Montgomery form c*2^64 mod p (the product is exactly x*c).
 
 Usage: python -m goldilocks_gb300.codegen   (rewrites csrc/gl_codelets.cuh)
 """
@@ -83,10 +84,11 @@ class Gen:
             k = (192 // order) * exp % 192
             return self.var("gl_shl<%d>(%s)" % (k, x))
         c = pow(root(order), exp, P)
-        return self.var("gl_mul(%s, 0x%016xull)" % (x, c))
+        return self.mulc(x, c)
 
     def mulc(self, x, c):
-        return self.var("gl_mul(%s, 0x%016xull)" % (x, c))
+        """x * c for a constant c: Montgomery product by c*2^64 mod p."""
+        return self.var("gl_mont_mul(%s, 0x%016xull)" % (x, c * 2**64 % P))
 
     # -- transforms on lists of variable names, natural order in/out --------
     def dft(self, xs):

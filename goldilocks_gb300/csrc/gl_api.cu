@@ -290,10 +290,12 @@ static int upload(gl_dev_tables &t, const std::vector<uint64_t> &h, uint64_t **d
   return GL_OK;
 }
 
-static std::vector<uint64_t> powers(uint64_t w, uint64_t count, uint64_t scale) {
+// scale * w^i for i < count, in Montgomery form (every table the pass kernels
+// multiply by is; see gl_mont_mul).
+static std::vector<uint64_t> mont_powers(uint64_t w, uint64_t count, uint64_t scale) {
   std::vector<uint64_t> v(count);
   uint64_t x = scale;
-  for (uint64_t i = 0; i < count; i++) { v[i] = x; x = h_mul(x, w); }
+  for (uint64_t i = 0; i < count; i++) { v[i] = gl_to_mont(x); x = h_mul(x, w); }
   return v;
 }
 
@@ -305,7 +307,7 @@ __global__ void gl_fill_pass_twiddles(uint64_t *out, const uint64_t *lo, const u
        i += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t k = i / n2, col = i % n2;
     const uint64_t e = col * k;  // < n1*n2
-    out[i] = gl_mul(lo[e & 4095], hi[e >> 12]);
+    out[i] = gl_tw2m(lo, hi, e);  // Montgomery form, like lo and hi
   }
 }
 
@@ -339,17 +341,17 @@ int gl_plan_tables(gl_plan *pl, gl_dev_tables **out) {
     st = gl_rader_tables(pl, t);
   } else if (pl->kind == 1) {
     for (int d = 0; d < 2 && st == GL_OK; d++)
-      st = upload(t, powers(h_root(n, d), n, 1), &t.blk[0][d]);
-    if (st == GL_OK) st = upload(t, powers(h_root(n, true), n, gl_inv(n % GL_P)), &t.blk_scaled_inv);
+      st = upload(t, mont_powers(h_root(n, d), n, 1), &t.blk[0][d]);
+    if (st == GL_OK) st = upload(t, mont_powers(h_root(n, true), n, gl_inv(n % GL_P)), &t.blk_scaled_inv);
   } else if (pl->kind == 2) {
     const uint64_t hi_count = (n + GL_TW_SPLIT - 1) / GL_TW_SPLIT;
     for (int d = 0; d < 2 && st == GL_OK; d++) {
-      st = upload(t, powers(h_root(pl->n1, d), pl->n1, 1), &t.blk[0][d]);
-      if (st == GL_OK) st = upload(t, powers(h_root(pl->n2, d), pl->n2, 1), &t.blk[1][d]);
+      st = upload(t, mont_powers(h_root(pl->n1, d), pl->n1, 1), &t.blk[0][d]);
+      if (st == GL_OK) st = upload(t, mont_powers(h_root(pl->n2, d), pl->n2, 1), &t.blk[1][d]);
       const uint64_t w = h_root(n, d);
       const uint64_t scale = d ? gl_inv(n % GL_P) : 1;
-      if (st == GL_OK) st = upload(t, powers(w, GL_TW_SPLIT, scale), &t.tw_lo[d]);
-      if (st == GL_OK) st = upload(t, powers(gl_pow(w, GL_TW_SPLIT), hi_count, 1), &t.tw_hi[d]);
+      if (st == GL_OK) st = upload(t, mont_powers(w, GL_TW_SPLIT, scale), &t.tw_lo[d]);
+      if (st == GL_OK) st = upload(t, mont_powers(gl_pow(w, GL_TW_SPLIT), hi_count, 1), &t.tw_hi[d]);
       if (st == GL_OK && n <= kFullTwiddleMax && full_twiddles_enabled()) {
         void *p = nullptr;
         cudaError_t e = cudaMalloc(&p, n * sizeof(uint64_t));
@@ -365,18 +367,18 @@ int gl_plan_tables(gl_plan *pl, gl_dev_tables **out) {
   } else if (pl->kind == 3) {
     const uint64_t n23 = pl->n2 * pl->n3;
     for (int d = 0; d < 2 && st == GL_OK; d++) {
-      st = upload(t, powers(h_root(pl->n1, d), pl->n1, 1), &t.blk[0][d]);
-      if (st == GL_OK) st = upload(t, powers(h_root(pl->n2, d), pl->n2, 1), &t.blk[1][d]);
-      if (st == GL_OK) st = upload(t, powers(h_root(pl->n3, d), pl->n3, 1), &t.blk3[d]);
+      st = upload(t, mont_powers(h_root(pl->n1, d), pl->n1, 1), &t.blk[0][d]);
+      if (st == GL_OK) st = upload(t, mont_powers(h_root(pl->n2, d), pl->n2, 1), &t.blk[1][d]);
+      if (st == GL_OK) st = upload(t, mont_powers(h_root(pl->n3, d), pl->n3, 1), &t.blk3[d]);
       const uint64_t w = h_root(n, d);
       const uint64_t scale = d ? gl_inv(n % GL_P) : 1;
-      if (st == GL_OK) st = upload(t, powers(w, GL_TW_SPLIT, scale), &t.tw_lo[d]);
+      if (st == GL_OK) st = upload(t, mont_powers(w, GL_TW_SPLIT, scale), &t.tw_lo[d]);
       if (st == GL_OK)
-        st = upload(t, powers(gl_pow(w, GL_TW_SPLIT), (n + GL_TW_SPLIT - 1) / GL_TW_SPLIT, 1), &t.tw_hi[d]);
+        st = upload(t, mont_powers(gl_pow(w, GL_TW_SPLIT), (n + GL_TW_SPLIT - 1) / GL_TW_SPLIT, 1), &t.tw_hi[d]);
       const uint64_t w23 = h_root(n23, d);
-      if (st == GL_OK) st = upload(t, powers(w23, GL_TW_SPLIT, 1), &t.tw23_lo[d]);
+      if (st == GL_OK) st = upload(t, mont_powers(w23, GL_TW_SPLIT, 1), &t.tw23_lo[d]);
       if (st == GL_OK)
-        st = upload(t, powers(gl_pow(w23, GL_TW_SPLIT), (n23 + GL_TW_SPLIT - 1) / GL_TW_SPLIT, 1),
+        st = upload(t, mont_powers(gl_pow(w23, GL_TW_SPLIT), (n23 + GL_TW_SPLIT - 1) / GL_TW_SPLIT, 1),
                     &t.tw23_hi[d]);
     }
   }
@@ -934,7 +936,7 @@ extern "C" int gl_ntt_columns(uint64_t *data, uint64_t rows, uint64_t cols, int 
   return st != GL_OK ? st : st2;
 }
 
-// Coset tables g^e (e < 4096) and g^(4096 e) (e < ceil(n/4096)), cached per
+// Coset tables g^e (e < 4096) and g^(4096 e) (e < ceil(n/4096)), Montgomery form, cached per
 // (device, g, n).
 static std::mutex g_coset_mu;
 static std::map<std::tuple<int, uint64_t, uint64_t>, std::pair<uint64_t *, uint64_t *>> g_coset;
@@ -949,9 +951,9 @@ static int coset_tables(uint64_t g, uint64_t n, const uint64_t **lo, const uint6
   if (it == g_coset.end()) {
     gl_dev_tables holder;
     uint64_t *a = nullptr, *b = nullptr;
-    int st = upload(holder, powers(g, GL_TW_SPLIT, 1), &a);
+    int st = upload(holder, mont_powers(g, GL_TW_SPLIT, 1), &a);
     if (st == GL_OK)
-      st = upload(holder, powers(gl_pow(g, GL_TW_SPLIT), (n + GL_TW_SPLIT - 1) / GL_TW_SPLIT, 1), &b);
+      st = upload(holder, mont_powers(gl_pow(g, GL_TW_SPLIT), (n + GL_TW_SPLIT - 1) / GL_TW_SPLIT, 1), &b);
     if (st != GL_OK) {
       for (void *p : holder.owned) cudaFree(p);
       return st;
@@ -1012,7 +1014,7 @@ __global__ void gl_coset_pad_kernel(const uint64_t *coef, uint64_t *dst, uint64_
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t j = i / cols;
-    dst[i] = j < n ? gl_mul(coef[i], gl_tw2(g_lo, g_hi, j)) : 0;
+    dst[i] = j < n ? gl_mont_mul(coef[i], gl_tw2m(g_lo, g_hi, j)) : 0;
   }
 }
 

@@ -214,6 +214,59 @@ GL_HD uint64_t gl_mul(uint64_t a, uint64_t b) {
 #endif
 }
 
+// Montgomery product a*w*2^-64 mod p, for twiddles and constants stored in
+// Montgomery form (w = t*2^64 mod p): then gl_mont_mul(a, w) = a*t mod p for
+// any word a, whatever representation a is in.  The reduction follows
+// mont_reduce_128 of ntt/src/field/algo/generic.rs:114-124: with the product
+// x = x1*2^64 + x0, a = x0 + (x0 << 32) (carry e), b = a - (a >> 32) - e,
+// result x1 - b (+ p on borrow).  b <= p - 1 for every x0, and x1 < p when
+// w < p, so the result is canonical without a final correction: 9 ALU
+// operations after the product against 18 for the canonical reduction.
+GL_HD uint64_t gl_mont_mul(uint64_t a, uint64_t w) {
+#ifdef GL_DEV_PTX
+  uint32_t a0, a1, b0, b1, l0, l1, h0, h1;
+  gl_unpack(a, a0, a1);
+  gl_unpack(w, b0, b1);
+  asm("mul.lo.u32 %0, %4, %6;\n\t"
+      "mul.hi.u32 %1, %4, %6;\n\t"
+      "mul.lo.u32 %2, %5, %7;\n\t"
+      "mul.hi.u32 %3, %5, %7;\n\t"
+      "mad.lo.cc.u32 %1, %4, %7, %1;\n\t"
+      "madc.hi.cc.u32 %2, %4, %7, %2;\n\t"
+      "addc.u32 %3, %3, 0;\n\t"
+      "mad.lo.cc.u32 %1, %5, %6, %1;\n\t"
+      "madc.hi.cc.u32 %2, %5, %6, %2;\n\t"
+      "addc.u32 %3, %3, 0;"
+      : "=&r"(l0), "=&r"(l1), "=&r"(h0), "=&r"(h1) : "r"(a0), "r"(a1), "r"(b0), "r"(b1));
+  // The carry of an add chain is not a borrow-in of a subtract chain, so e
+  // is taken into s = a_hi + e first (no overflow: a_hi <= 2^32 - 2 when e = 1).
+  uint32_t ah, sh, c0, c1, r0, r1, m;
+  asm("add.cc.u32 %2, %8, %7;\n\t"       // a_hi = l1 + l0, carry e
+      "addc.u32 %3, %2, 0;\n\t"          // s = a_hi + e
+      "sub.cc.u32 %4, %7, %3;\n\t"       // b = (a_hi : l0) - s
+      "subc.u32 %5, %2, 0;\n\t"
+      "sub.cc.u32 %0, %9, %4;\n\t"       // r = x1 - b
+      "subc.cc.u32 %1, %10, %5;\n\t"
+      "subc.u32 %6, 0, 0;\n\t"           // borrow: + p = - EPS (mod 2^64)
+      "sub.cc.u32 %0, %0, %6;\n\t"
+      "subc.u32 %1, %1, 0;"
+      : "=&r"(r0), "=&r"(r1), "=&r"(ah), "=&r"(sh), "=&r"(c0), "=&r"(c1), "=&r"(m)
+      : "r"(l0), "r"(l1), "r"(h0), "r"(h1));
+  return gl_pack(r0, r1);
+#else
+  const unsigned __int128 x = (unsigned __int128)a * w;
+  const uint64_t x0 = (uint64_t)x, x1 = (uint64_t)(x >> 64);
+  const uint64_t s = x0 + (x0 << 32);
+  const uint64_t e = s < x0;
+  const uint64_t b = s - (s >> 32) - e;
+  const uint64_t r = x1 - b;
+  return x1 < b ? r - GL_EPS : r;
+#endif
+}
+
+// t*2^64 mod p: the Montgomery form of t (tables of gl_mont_mul factors).
+GL_HD uint64_t gl_to_mont(uint64_t t) { return gl_mul(t, GL_EPS); }
+
 // x * 2^K mod p for a compile-time K in [0, 192).
 template <int K>
 GL_HD uint64_t gl_shl(uint64_t x) {

@@ -69,7 +69,7 @@ __device__ __forceinline__ void gl_gen_round1(const gl_pass_args &a, const gl_ge
 #pragma unroll
       for (int t = 0; t < R; t++) {
         const uint64_t j = (uint64_t)(g + q.S1 * t);
-        if (j < a.in_limit) x[t] = gl_mul(x[t], gl_tw2(a.itw_lo, a.itw_hi, j * a.itw_jmul + col));
+        if (j < a.in_limit) x[t] = gl_mont_mul(x[t], gl_tw2m(a.itw_lo, a.itw_hi, j * a.itw_jmul + col));
       }
     }
     gl_dft<R, INV>(x);
@@ -79,8 +79,8 @@ __device__ __forceinline__ void gl_gen_round1(const gl_pass_args &a, const gl_ge
         const uint64_t col = (uint64_t)lane / a.tw_lane_div;
 #pragma unroll
         for (int t = 0; t < R; t++) {
-          uint64_t v = scale_all ? gl_mul(x[t], a.tw_m[0]) : x[t];
-          if (a.flags & GL_PF_PASS_TWIDDLE) v = gl_mul(v, gl_pass_tw(a, col, t));
+          uint64_t v = scale_all ? gl_mont_mul(x[t], a.tw_m[0]) : x[t];
+          if (a.flags & GL_PF_PASS_TWIDDLE) v = gl_mont_mul(v, gl_pass_tw(a, col, t));
           if (a.flags & GL_PF_OUT_MUL) v = gl_out_mul(a, q.mul, lane, t, v);
           dst[(int64_t)t * a.out_is] = v;
         }
@@ -89,7 +89,7 @@ __device__ __forceinline__ void gl_gen_round1(const gl_pass_args &a, const gl_ge
 #pragma unroll
       for (int t = 0; t < R; t++) {
         uint64_t v = x[t];
-        if (t > 0 || scale_all) v = gl_mul(v, __ldg(a.tw_m + g * t));
+        if (t > 0 || scale_all) v = gl_mont_mul(v, __ldg(a.tw_m + g * t));
         sm[c * q.LS + g + q.S1 * t] = v;
       }
     }
@@ -113,7 +113,7 @@ __device__ __forceinline__ void gl_gen_round2(const gl_pass_args &a, const gl_ge
 #pragma unroll
     for (int t = 0; t < R; t++) {
       uint64_t v = x[t];
-      if (t > 0) v = gl_mul(v, __ldg(a.tw_r2 + q.R1 * d3 * t));
+      if (t > 0) v = gl_mont_mul(v, __ldg(a.tw_r2 + q.R1 * d3 * t));
       sm[base + q.R3 * t] = v;
     }
   }
@@ -150,7 +150,7 @@ __device__ __forceinline__ void gl_gen_round_last(const gl_pass_args &a, const g
       for (int t = 0; t < R; t++) {
         const uint64_t k = (uint64_t)(kbase + SL * t);
         uint64_t v = x[t];
-        if (a.flags & GL_PF_PASS_TWIDDLE) v = gl_mul(v, gl_pass_tw(a, col, k));
+        if (a.flags & GL_PF_PASS_TWIDDLE) v = gl_mont_mul(v, gl_pass_tw(a, col, k));
         if (a.flags & GL_PF_OUT_MUL) v = gl_out_mul(a, q.mul, lane, (int64_t)k, v);
         dst[(int64_t)k * a.out_is] = v;
       }

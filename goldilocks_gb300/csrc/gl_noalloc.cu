@@ -55,7 +55,8 @@ int device_ptrs(noalloc_ptrs *out) {
   return GL_OK;
 }
 
-// Writes every table word the two passes read (nothing is assumed zero).
+// Writes every table word the two passes read (nothing is assumed zero), in
+// the Montgomery form the pass kernels multiply by.
 __global__ void fill_tables(uint64_t *tab, uint64_t w1, uint32_t n1, uint64_t w2, uint32_t n2,
                             uint64_t w, uint64_t scale, uint32_t hi_count) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < GL_NOALLOC_TAB_WORDS;
@@ -70,7 +71,7 @@ __global__ void fill_tables(uint64_t *tab, uint64_t w1, uint32_t n1, uint64_t w2
     } else if (i - GL_NOALLOC_THI < hi_count) {
       v = gl_pow(w, 4096ull * (i - GL_NOALLOC_THI));
     }
-    tab[i] = v;
+    tab[i] = gl_to_mont(v);
   }
 }
 

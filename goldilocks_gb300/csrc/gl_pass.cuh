@@ -62,11 +62,20 @@ struct gl_pass_args {
   int64_t mul_ls, mul_bs, mul_bs2;
 };
 
-// Pass twiddle omega_n^(col*k): from the full table when present, else from
-// the two-level table (two loads, one extra multiplication).
+// Every table a pass kernel multiplies by (tw_m, tw_r2, tw_lo/hi, tw_full,
+// itw_lo/hi) holds Montgomery forms t*2^64 mod p, and the kernels multiply
+// with gl_mont_mul: the product is exactly a*t, in 8 fewer ALU operations.
+
+// Pass twiddle omega_n^(col*k) (Montgomery form): from the full table when
+// present, else from the two-level table (two loads, one extra product).
 __device__ __forceinline__ uint64_t gl_pass_tw(const gl_pass_args &a, uint64_t col, uint64_t k) {
   if (a.flags & GL_PF_TW_TABLE) return __ldg(a.tw_full + (int64_t)k * a.tw_ld + (int64_t)col);
-  return gl_mul(a.tw_lo[(col * k) & 4095], a.tw_hi[(col * k) >> 12]);
+  return gl_mont_mul(a.tw_lo[(col * k) & 4095], a.tw_hi[(col * k) >> 12]);
+}
+
+// lo[e & 4095] * hi[e >> 12] from two-level Montgomery tables (Montgomery form).
+__device__ __forceinline__ uint64_t gl_tw2m(const uint64_t *lo, const uint64_t *hi, uint64_t e) {
+  return gl_mont_mul(lo[e & 4095], hi[e >> 12]);
 }
 
 // Pointwise factor on the final store; `mb` is mul + by*mul_bs + bz*mul_bs2.
@@ -126,7 +135,7 @@ gl_pass_kernel(const gl_pass_args a) {
 #pragma unroll
       for (int jA = 0; jA < MA; jA++) {
         const uint64_t j = (uint64_t)(MB * jA + jB);
-        if (j < a.in_limit) x[jA] = gl_mul(x[jA], gl_tw2(a.itw_lo, a.itw_hi, j * a.itw_jmul + col));
+        if (j < a.in_limit) x[jA] = gl_mont_mul(x[jA], gl_tw2m(a.itw_lo, a.itw_hi, j * a.itw_jmul + col));
       }
     }
   }
@@ -134,11 +143,11 @@ gl_pass_kernel(const gl_pass_args a) {
   if constexpr (MB > 1) {
 #pragma unroll
     for (int kA = 0; kA < MA; kA++)
-      if (kA > 0 || scale_all) x[kA] = gl_mul(x[kA], a.tw_m[jB * kA]);
+      if (kA > 0 || scale_all) x[kA] = gl_mont_mul(x[kA], a.tw_m[jB * kA]);
   } else if (scale_all) {
     const uint64_t s = a.tw_m[0];
 #pragma unroll
-    for (int kA = 0; kA < MA; kA++) x[kA] = gl_mul(x[kA], s);
+    for (int kA = 0; kA < MA; kA++) x[kA] = gl_mont_mul(x[kA], s);
   }
 
   if constexpr (MB == 1) {
@@ -149,7 +158,7 @@ gl_pass_kernel(const gl_pass_args a) {
         const uint64_t col = (uint64_t)(lane0 + c) / a.tw_lane_div;
 #pragma unroll
         for (int kA = 0; kA < MA; kA++)
-          dst[(int64_t)kA * a.out_is] = gl_mul(x[kA], gl_tw2(a.tw_lo, a.tw_hi, col * kA));
+          dst[(int64_t)kA * a.out_is] = gl_mont_mul(x[kA], gl_pass_tw(a, col, kA));
       } else if (a.flags & GL_PF_OUT_MUL) {
         const uint64_t *mb = a.mul + blockIdx.y * a.mul_bs + blockIdx.z * a.mul_bs2;
 #pragma unroll
@@ -183,7 +192,7 @@ gl_pass_kernel(const gl_pass_args a) {
 #pragma unroll
           for (int kB = 0; kB < MB; kB++) {
             const uint64_t k = (uint64_t)(kA + MA * kB);
-            dst[(int64_t)k * a.out_is] = gl_mul(y[kB], gl_tw2(a.tw_lo, a.tw_hi, col * k));
+            dst[(int64_t)k * a.out_is] = gl_mont_mul(y[kB], gl_pass_tw(a, col, k));
           }
         } else if (a.flags & GL_PF_OUT_MUL) {
           const uint64_t *mb = a.mul + blockIdx.y * a.mul_bs + blockIdx.z * a.mul_bs2;

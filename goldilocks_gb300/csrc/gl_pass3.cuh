@@ -87,7 +87,7 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
 #pragma unroll
         for (int t = 0; t < R1; t++) {
           const uint64_t j = (uint64_t)(g + S1 * t);
-          if (j < a.in_limit) x[t] = gl_mul(x[t], gl_tw2(a.itw_lo, a.itw_hi, j * a.itw_jmul + col));
+          if (j < a.in_limit) x[t] = gl_mont_mul(x[t], gl_tw2m(a.itw_lo, a.itw_hi, j * a.itw_jmul + col));
         }
       }
       gl_dft<R1, INV>(x);
@@ -96,7 +96,7 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
         if (scale_all) {
           const uint64_t s = a.tw_m[0];
 #pragma unroll
-          for (int t = 0; t < R1; t++) x[t] = gl_mul(x[t], s);
+          for (int t = 0; t < R1; t++) x[t] = gl_mont_mul(x[t], s);
         }
         if (live) {
           uint64_t *dst = out + lane * a.out_ls;
@@ -104,7 +104,7 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
             const uint64_t col = (uint64_t)lane / a.tw_lane_div;
 #pragma unroll
             for (int t = 0; t < R1; t++)
-              dst[(int64_t)t * a.out_is] = gl_mul(x[t], gl_pass_tw(a, col, t));
+              dst[(int64_t)t * a.out_is] = gl_mont_mul(x[t], gl_pass_tw(a, col, t));
           } else if (a.flags & GL_PF_OUT_MUL) {
             const uint64_t *mb = a.mul + by * a.mul_bs + bz * a.mul_bs2;
 #pragma unroll
@@ -118,7 +118,7 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
 #pragma unroll
         for (int t = 0; t < R1; t++) {
           uint64_t v = x[t];
-          if (t > 0 || scale_all) v = gl_mul(v, __ldg(a.tw_m + g * t));
+          if (t > 0 || scale_all) v = gl_mont_mul(v, __ldg(a.tw_m + g * t));
           sm[L::word(c, g + S1 * t)] = v;
         }
       }
@@ -141,7 +141,7 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
 #pragma unroll
       for (int t = 0; t < R2; t++) {
         uint64_t v = x[t];
-        if (t > 0) v = gl_mul(v, __ldg(a.tw_r2 + R1 * d3 * t));
+        if (t > 0) v = gl_mont_mul(v, __ldg(a.tw_r2 + R1 * d3 * t));
         sm[L::word(c, base + R3 * t)] = v;
       }
     }
@@ -180,7 +180,7 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
 #pragma unroll
           for (int t = 0; t < RL; t++) {
             const uint64_t k = (uint64_t)(kbase + SL * t);
-            dst[(int64_t)k * a.out_is] = gl_mul(x[t], gl_pass_tw(a, col, k));
+            dst[(int64_t)k * a.out_is] = gl_mont_mul(x[t], gl_pass_tw(a, col, k));
           }
         } else if (a.flags & GL_PF_OUT_MUL) {
           const uint64_t *mb = a.mul + by * a.mul_bs + bz * a.mul_bs2;

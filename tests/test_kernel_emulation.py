@@ -37,9 +37,11 @@ def root(n, inv=False):
 
 
 def table(w, count, scale=1):
+    """scale * w^i, i < count, in the Montgomery form (x * 2^64 mod p) the pass
+    kernels multiply by."""
     out, x = [], scale
     for _ in range(count):
-        out.append(x)
+        out.append(x * 2**64 % P)
         x = x * w % P
     return np.array(out, dtype=np.uint64)
 
