@@ -267,13 +267,35 @@ GL_HD uint64_t gl_mont_mul(uint64_t a, uint64_t w) {
 // t*2^64 mod p: the Montgomery form of t (tables of gl_mont_mul factors).
 GL_HD uint64_t gl_to_mont(uint64_t t) { return gl_mul(t, GL_EPS); }
 
-// x * 2^K mod p for a compile-time K in [0, 192).
+// 2^(k + 64) mod p, the Montgomery form of 2^k, at compile time.
+GL_HD constexpr uint64_t gl_pow2_mont(int k) {
+  uint64_t x = GL_EPS;  // 2^64 mod p
+  for (int i = 0; i < k; i++) {
+    const uint64_t d = x << 1;
+    x = (x >> 63) ? d + GL_EPS : d;   // 2^64 = EPS (mod p); no second wrap: d <= 2^64 - 2^33
+    if (x >= GL_P) x -= GL_P;
+  }
+  return x;
+}
+
+// x * 2^K mod p for a compile-time K in [0, 192).  By default a Montgomery
+// product by the constant 2^(K+64) mod p: about 11 operations on the integer
+// ALU pipe plus 8 multiply-adds on the FMA pipe, against about 21 ALU
+// operations for the word shifts and the canonical reduction below
+// (GL_SHL_WORDS) -- the ALU pipe is what bounds the transforms.
 template <int K>
 GL_HD uint64_t gl_shl(uint64_t x) {
   static_assert(K >= 0 && K < 192, "shift out of range");
   if constexpr (K == 0) {
     return x;
-  } else if constexpr (K >= 96) {
+  } else if constexpr (K == 96) {
+    return gl_neg(x);                     // 2^96 = -1
+#if defined(GL_DEV_PTX) && !defined(GL_SHL_WORDS)
+  } else if constexpr (true) {
+    constexpr uint64_t c = gl_pow2_mont(K);
+    return gl_mont_mul(x, c);
+#endif
+  } else if constexpr (K > 96) {
     return gl_neg(gl_shl<K - 96>(x));     // 2^96 = -1
   } else {
 #ifdef GL_DEV_PTX
