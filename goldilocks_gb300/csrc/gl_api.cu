@@ -181,16 +181,25 @@ static bool use_two_lane_passes() {
 
 const gl_kernel_entry *gl_find_kernel(uint64_t m, bool full, bool inv) {
   size_t cnt = 0;
-  if (!full && use_two_lane_passes()) {
+  if (full) {
+    const gl_kernel_entry *e = inv ? gl_kernels_full_inv(&cnt) : gl_kernels_full_fwd(&cnt);
+    if (const gl_kernel_entry *k = find_in(e, cnt, m)) return k;
+    return generic_entry(m, inv);
+  }
+  if (use_two_lane_passes()) {
     const gl_kernel_entry *e = inv ? gl_kernels_pass2_inv(&cnt) : gl_kernels_pass2_fwd(&cnt);
     if (const gl_kernel_entry *k = find_in(e, cnt, m)) return k;
   }
-  if (!full && use_wide_kernels()) {
+  return gl_find_kernel4(m, inv);
+}
+
+const gl_kernel_entry *gl_find_kernel4(uint64_t m, bool inv) {
+  size_t cnt = 0;
+  if (use_wide_kernels()) {
     const gl_kernel_entry *e = inv ? gl_kernels_wide_inv(&cnt) : gl_kernels_wide_fwd(&cnt);
     if (const gl_kernel_entry *k = find_in(e, cnt, m)) return k;
   }
-  const gl_kernel_entry *e = full ? (inv ? gl_kernels_full_inv(&cnt) : gl_kernels_full_fwd(&cnt))
-                                  : (inv ? gl_kernels_pass_inv(&cnt) : gl_kernels_pass_fwd(&cnt));
+  const gl_kernel_entry *e = inv ? gl_kernels_pass_inv(&cnt) : gl_kernels_pass_fwd(&cnt);
   if (const gl_kernel_entry *k = find_in(e, cnt, m)) return k;
   return generic_entry(m, inv);  // every other size up to 4096 with radices <= 17
 }
@@ -243,6 +252,8 @@ static void choose_schedule(gl_plan *pl) {
     for (int d = 0; d < 2; d++) {
       pl->k[0][d] = gl_find_kernel(pl->n1, false, d == 1);
       pl->k[1][d] = gl_find_kernel(pl->n2, false, d == 1);
+      pl->k4[0][d] = gl_find_kernel4(pl->n1, d == 1);
+      pl->k4[1][d] = gl_find_kernel4(pl->n2, d == 1);
     }
     return;
   }
@@ -273,6 +284,8 @@ static void choose_schedule(gl_plan *pl) {
       pl->k[0][d] = gl_find_kernel(pl->n1, false, d == 1);
       pl->k[1][d] = gl_find_kernel(pl->n2, false, d == 1);
       pl->k[2][d] = gl_find_kernel(pl->n3, false, d == 1);
+      for (int s = 0; s < 3; s++)
+        pl->k4[s][d] = gl_find_kernel4(s == 0 ? pl->n1 : s == 1 ? pl->n2 : pl->n3, d == 1);
     }
     return;
   }
@@ -637,7 +650,8 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
     //   C  per (k1, k2): n3-point over j3, stored at k         scratch -> dst
     // (a column pass writes exactly the positions it reads, so B is in place).
     const uint64_t n1 = pl->n1, n2 = pl->n2, n3 = pl->n3, n23 = n2 * n3;
-    const gl_kernel_entry *ka = pl->k[0][d], *kb = pl->k[1][d], *kcr = pl->k[2][d];
+    const auto &ks = C > 1 ? pl->k4 : pl->k;  // interleaved columns: four-lane kernels
+    const gl_kernel_entry *ka = ks[0][d], *kb = ks[1][d], *kcr = ks[2][d];
     for (uint64_t b = 0; b < B; b++) {
       const uint64_t *in = src + b * bs;
       uint64_t *out = dst + b * bs;
@@ -698,7 +712,8 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
   }
   // Four-step: n = n1*n2, j = n2*j1 + j2, k = k1 + n1*k2.
   const uint64_t n1 = pl->n1, n2 = pl->n2;
-  const gl_kernel_entry *kc = pl->k[0][d], *kr = pl->k[1][d];
+  const auto &ks = C > 1 ? pl->k4 : pl->k;  // interleaved columns: four-lane kernels
+  const gl_kernel_entry *kc = ks[0][d], *kr = ks[1][d];
   for (uint64_t off = 0; off < B; off += kMaxGridYZ) {
     const uint64_t cb = std::min(kMaxGridYZ, B - off);
     // COL: lanes are (j2, c) pairs, contiguous; n1-point transforms down them.

@@ -51,6 +51,8 @@ inline uint64_t gl_tiles(uint64_t lanes, const gl_kernel_entry *k) { return (lan
 
 // Launch-time check: the kernel entry for (m, full, inv), or nullptr.
 const gl_kernel_entry *gl_find_kernel(uint64_t m, bool full, bool inv);
+// The pass kernel for m with four lanes per CTA (or the run-time-radix one).
+const gl_kernel_entry *gl_find_kernel4(uint64_t m, bool inv);
 
 #define GL_PASS_LANES 4  // pass sizes are multiples of it; every pass kernel's lanes divide it
 #define GL_TW_SPLIT 4096  // two-level pass twiddle: e = hi*4096 + lo
@@ -86,6 +88,9 @@ struct gl_plan {
   gl_plan *pq = nullptr;    // kind 4: plan of q - 1 (the cyclic convolution)
   gl_plan *pm = nullptr;    // kind 4: plan of m = size / q (may itself be kind 4)
   const gl_kernel_entry *k[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};  // [stage][dir]
+  // The same stages with four-lane kernels, for interleaved columns (C > 1):
+  // there a two-lane CTA reads and writes 16-byte row pieces.
+  const gl_kernel_entry *k4[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
   std::string tree;
   std::mutex mu;
   std::map<int, gl_dev_tables> dev;  // per device id
