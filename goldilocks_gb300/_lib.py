@@ -37,6 +37,7 @@ SIGNATURES = [
     ("gl_coset_lde", _int, [_vp, _vp, _u64, _u64, _u32, _u64, _int, _vp]),
     ("gl_convolve", _int, [_vp, _vp, _u64, _u64, _u64, _int, _int, _vp]),
     ("gl_host_pipeline", _int, [_vp, _u64, _u32]),
+    ("gl_batch_wait_selftest", _int, [_u64, ctypes.POINTER(_u32)]),
     ("gl_k12_next_layer_size", _u64, [_u64]),
     ("gl_merkle_tree_bytes", _u64, [_u64]),
     ("gl_k12_process_layer", _int, [_vp, _u64, _vp, _int, _vp]),

@@ -519,3 +519,36 @@ extern "C" int gl_batch_autotune(const gl_poly *polys, uint64_t count, int reps,
   g_tuned[batch_shape(polys, count)] = best_mode;
   return GL_OK;
 }
+
+// Diagnostic: one row-pass work item whose column pass is never queued, so
+// its bounded wait must run out.  The kernel records GL_ERR_TIMEOUT and every
+// CTA returns; the item itself is never executed.
+extern "C" int gl_batch_wait_selftest(uint64_t wait_ns, uint32_t *status) {
+  if (!status) return GL_ERR_INVALID;
+  wait_ns = std::min<uint64_t>(std::max<uint64_t>(wait_ns, 1000000ull), 2000000000ull);
+  const gl_work item{0u, 2u, 0u, 0u, 0u, 1u};  // needs one finished column tile of poly 0
+  const size_t o_args = 0, o_items = 256, o_ctr = 512;
+  dev_block blk;
+  blk.s = nullptr;
+  cudaError_t e = cudaMalloc(&blk.p, 1024);
+  if (e != cudaSuccess) return gl_cuda_status(e);
+  char *base = (char *)blk.p;
+  gl_pass_args args{};
+  if ((e = cudaMemcpy(base + o_args, &args, sizeof(args), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(base + o_items, &item, sizeof(item), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemset(base + o_ctr, 0, 3 * sizeof(uint32_t))) != cudaSuccess) {
+    cudaFree(blk.p);
+    blk.p = nullptr;
+    return gl_cuda_status(e);
+  }
+  uint32_t *ctr = (uint32_t *)(base + o_ctr);
+  const size_t smem = max_shape_smem();
+  cudaFuncSetAttribute(gl_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  gl_batch_kernel<<<1, kNT, smem>>>((const gl_work *)(base + o_items), 1u, (const gl_pass_args *)(base + o_args),
+                                    ctr, ctr + 2, ctr + 1, wait_ns);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(status, ctr + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  cudaFree(blk.p);
+  blk.p = nullptr;
+  return gl_cuda_status(e);
+}

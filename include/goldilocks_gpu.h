@@ -223,6 +223,13 @@ int gl_batch_execute(const gl_poly *polys, uint64_t count, int mode, void *strea
  * The polynomials are transformed (1 + reps) times per mode. */
 int gl_batch_autotune(const gl_poly *polys, uint64_t count, int reps, void *stream, double *ms_out);
 
+/* Diagnostic for the persistent kernel's bounded waits: runs it on one work
+ * item whose dependency is never satisfied, with the wait limited to wait_ns
+ * (clamped to 1 ms .. 2 s); *status receives the kernel's error word, which
+ * must be GL_ERR_TIMEOUT.  The GPU context stays usable afterwards.
+ * Synchronous. */
+int gl_batch_wait_selftest(uint64_t wait_ns, uint32_t *status);
+
 /* ---- continuous-batching request server (no counterpart in the reference) ---- */
 
 enum { GL_OP_NTT = 0, GL_OP_INTT = 1, GL_OP_LDE = 2 };

@@ -52,3 +52,22 @@ def test_autotune_picks_a_mode(gl, cuda):
     assert set(ms) == {"persistent", "buckets", "per_call"} and all(v > 0 for v in ms.values())
     _, items2 = make_batch(cuda, sizes, seed=9)
     B.run(items2, mode=B.AUTO)
+
+
+def test_bounded_wait_reports_timeout_and_context_survives(gl, oracle, cuda):
+    """A row item whose column pass never runs: the persistent kernel's wait
+    gives up after the limit, reports GL_ERR_TIMEOUT, and the GPU context keeps
+    working (no fault, no hang)."""
+    import ctypes
+    import time
+    L = gl._lib
+    st = ctypes.c_uint32(0)
+    t0 = time.perf_counter()
+    assert L.load().gl_batch_wait_selftest(50_000_000, ctypes.byref(st)) == L.GL_OK   # 50 ms
+    elapsed = time.perf_counter() - t0
+    assert st.value == L.GL_ERR_TIMEOUT
+    assert 0.04 < elapsed < 5.0
+    x = gl.fill_uniform(1 << 16, seed=9)
+    d = cuda.tensor(x.view(np.int64), device="cuda")
+    gl.ntt(d)
+    assert np.array_equal(d.cpu().numpy().view(np.uint64), oracle.ntt(x))
