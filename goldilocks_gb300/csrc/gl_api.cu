@@ -768,6 +768,50 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
   return gl_cuda_status(cudaGetLastError());
 }
 
+// One pass of a two-pass plan over lanes [lo, hi) of one contiguous
+// transform, with the arguments gl_enqueue_transform gives the whole pass:
+// stage 0 is the column pass src -> scratch (lanes are the columns j2),
+// stage 1 the row pass scratch -> dst (lanes are the rows k1).  Lets a caller
+// start the column pass on the columns that have arrived and copy out the
+// output columns whose row pass is done.
+int gl_enqueue_pass_range(gl_plan *pl, int stage, const uint64_t *src, uint64_t *dst, uint64_t lo,
+                          uint64_t hi, bool inv, cudaStream_t stream) {
+  if (pl->kind != 2 || stage < 0 || stage > 1 || lo >= hi) return GL_ERR_INVALID;
+  gl_dev_tables *t = nullptr;
+  int st = gl_plan_tables(pl, &t);
+  if (st != GL_OK) return st;
+  const int d = inv ? 1 : 0;
+  const uint64_t n1 = pl->n1, n2 = pl->n2;
+  gl_pass_args a{};
+  a.in_limit = 0xffffffffu;
+  a.tw_lane_div = 1;
+  a.lanes = (uint32_t)(hi - lo);
+  if (stage == 0) {
+    if (hi > n2) return GL_ERR_INVALID;
+    const gl_kernel_entry *kc = pl->k[0][d];
+    a.in = src + lo; a.out = dst + lo;
+    a.in_ls = a.out_ls = 1; a.in_is = a.out_is = (int64_t)n2;
+    a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
+    a.tw_m = a.tw_r2 = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
+    a.tw_col0 = lo;
+    if (t->tw_full[d]) {
+      a.flags |= GL_PF_TW_TABLE;
+      a.tw_full = t->tw_full[d];
+      a.tw_ld = (int64_t)n2;
+    }
+    gl_launch(kc, 1, a, dim3((unsigned)gl_tiles(hi - lo, kc)), n1 * (hi - lo), stream);
+  } else {
+    if (hi > n1) return GL_ERR_INVALID;
+    const gl_kernel_entry *kr = pl->k[1][d];
+    a.in = src + lo * n2; a.out = dst + lo;
+    a.in_ls = (int64_t)n2; a.in_is = 1; a.out_ls = 1; a.out_is = (int64_t)n1;
+    a.flags = GL_PF_STORE_LANE_FAST;
+    a.tw_m = a.tw_r2 = t->blk[1][d];
+    gl_launch(kr, 2, a, dim3((unsigned)gl_tiles(hi - lo, kr)), n2 * (hi - lo), stream);
+  }
+  return gl_cuda_status(cudaGetLastError());
+}
+
 static int run_device(gl_plan *pl, uint64_t *data, uint64_t count, bool inv, uint64_t *scratch,
                       cudaStream_t stream) {
   return gl_enqueue_transform(pl, data, data, 1, count, pl->size, inv, scratch, stream);

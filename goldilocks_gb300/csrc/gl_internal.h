@@ -122,6 +122,12 @@ struct gl_store_mul {
   bool mont = false;
 };
 
+// One pass of a two-pass plan (kind 2) over lanes [lo, hi) of a single
+// contiguous transform: stage 0 column pass src -> scratch, stage 1 row pass
+// scratch -> dst.  (gl_api.cu)
+int gl_enqueue_pass_range(gl_plan *pl, int stage, const uint64_t *src, uint64_t *dst, uint64_t lo,
+                          uint64_t hi, bool inv, cudaStream_t stream);
+
 // Device address of page-locked, device-mapped host memory [p, p + bytes), or
 // nullptr (then host data is staged through device memory).  (gl_api.cu)
 void *gl_host_device_view(const void *p, uint64_t bytes);

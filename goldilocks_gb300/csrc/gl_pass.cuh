@@ -56,6 +56,7 @@ struct gl_pass_args {
   const uint64_t *const *in_ptrs;  // GL_PF_PTR_TABLE: base pointer of batch item by
   uint64_t *const *out_ptrs;
   int32_t gen_r[3];                 // run-time radices of gl_generic_kernel
+  uint64_t tw_col0;                 // pass twiddle column of lane 0 (a launch over a lane range)
   // GL_PF_OUT_MUL: the factor of output k of lane `lane` in batch item (by, bz)
   // is mul[by*mul_bs + bz*mul_bs2 + lane*mul_ls + k*out_is].
   const uint64_t *mul;
@@ -69,6 +70,7 @@ struct gl_pass_args {
 // Pass twiddle omega_n^(col*k) (Montgomery form): from the full table when
 // present, else from the two-level table (two loads, one extra product).
 __device__ __forceinline__ uint64_t gl_pass_tw(const gl_pass_args &a, uint64_t col, uint64_t k) {
+  col += a.tw_col0;
   if (a.flags & GL_PF_TW_TABLE) return __ldg(a.tw_full + (int64_t)k * a.tw_ld + (int64_t)col);
   return gl_mont_mul(a.tw_lo[(col * k) & 4095], a.tw_hi[(col * k) >> 12]);
 }

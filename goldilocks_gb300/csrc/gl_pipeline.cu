@@ -2,7 +2,10 @@
 // reference, whose transforms run where the data lives).
 //
 // Each job is one round trip: its buffer is copied to the device once, gets
-// every transform of its op list there, and is copied back once.  Three
+// every transform of its op list there, and is copied back once.  A large
+// two-pass transform moves in column blocks (2D copies): its column pass
+// starts on the blocks that have arrived and its last row pass hands output
+// blocks to the copy-out stream as they finish.  Three
 // streams per device -- copy-in, compute, copy-out -- with a ring of `depth`
 // device slots, so job i+1 is copied in while job i computes and job i-1 is
 // copied out.  The host-device link carries both directions at once (on
@@ -42,6 +45,9 @@ int streams_for_device(pipe_streams **out) {
   *out = it->second;
   return GL_OK;
 }
+
+constexpr int kChunks = 8;                       // column blocks of a chunked transform
+constexpr uint64_t kChunkMinWords = 1ull << 21;   // 16 MiB: smaller jobs move whole
 
 struct events {
   std::vector<cudaEvent_t> ev;
@@ -94,11 +100,67 @@ extern "C" int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_
   cudaEventRecord(alloc.ev[0], ps->comp);  // the block exists for the copy streams
   cudaStreamWaitEvent(ps->in, alloc.ev[0], 0);
   uint64_t *scratch = block + depth * slot_words;
+  std::vector<cudaEvent_t> chunk_ev;  // per chunked job: kChunks copy-ins, then kChunks row passes
   for (uint64_t i = 0; i < njobs && st == GL_OK; i++) {
     const gl_host_job &j = jobs[i];
+    gl_plan *pl = plans[i];
     uint64_t *buf = block + (i % depth) * slot_words;
     const uint64_t words_i = j.len * j.count;
     if (i >= depth) cudaStreamWaitEvent(ps->in, freed.ev[i - depth], 0);  // slot copied out
+    // A large two-pass transform is moved in column blocks: its column pass
+    // starts on the blocks that have arrived, and the blocks of the output
+    // whose row pass is done are copied out while the rest computes.
+    const bool chunked = pl->kind == 2 && j.count == 1 && j.nops > 0 && words_i >= kChunkMinWords &&
+                         pl->n1 % kChunks == 0 && pl->n2 % kChunks == 0;
+    if (chunked) {
+      const uint64_t n1 = pl->n1, n2 = pl->n2, w2 = n2 / kChunks, w1 = n1 / kChunks;
+      const size_t base_ev = chunk_ev.size();
+      for (int q = 0; q < 2 * kChunks; q++) {
+        cudaEvent_t ev;
+        if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) break;
+        chunk_ev.push_back(ev);
+      }
+      if (e != cudaSuccess) { st = gl_cuda_status(e); break; }
+      // rows j1 (n1 of them) of n2 words; column block q = columns [q w2, (q+1) w2)
+      for (int q = 0; q < kChunks && e == cudaSuccess; q++) {
+        e = cudaMemcpy2DAsync(buf + q * w2, n2 * 8, j.data + q * w2, n2 * 8, w2 * 8, n1,
+                              cudaMemcpyHostToDevice, ps->in);
+        cudaEventRecord(chunk_ev[base_ev + q], ps->in);
+      }
+      if (e != cudaSuccess) { st = gl_cuda_status(e); break; }
+      cudaEventRecord(ready.ev[i], ps->in);
+      for (uint32_t k = 0; k < j.nops && st == GL_OK; k++) {
+        const bool inv = j.dirs[k] == GL_INVERSE;
+        if (k == 0) {
+          for (int q = 0; q < kChunks && st == GL_OK; q++) {
+            cudaStreamWaitEvent(ps->comp, chunk_ev[base_ev + q], 0);
+            st = gl_enqueue_pass_range(pl, 0, buf, scratch, q * w2, (q + 1) * w2, inv, ps->comp);
+          }
+        } else {
+          st = gl_enqueue_pass_range(pl, 0, buf, scratch, 0, n2, inv, ps->comp);
+        }
+        if (st != GL_OK) break;
+        if (k + 1 < j.nops) {
+          st = gl_enqueue_pass_range(pl, 1, scratch, buf, 0, n1, inv, ps->comp);
+        } else {
+          // output (k2, k1) at k2*n1 + k1: the row pass over rows [r w1, (r+1) w1)
+          // writes output column block r
+          for (int r = 0; r < kChunks && st == GL_OK; r++) {
+            st = gl_enqueue_pass_range(pl, 1, scratch, buf, r * w1, (r + 1) * w1, inv, ps->comp);
+            cudaEventRecord(chunk_ev[base_ev + kChunks + r], ps->comp);
+          }
+        }
+      }
+      cudaEventRecord(done.ev[i], ps->comp);
+      for (int r = 0; r < kChunks && st == GL_OK && e == cudaSuccess; r++) {
+        cudaStreamWaitEvent(ps->out, chunk_ev[base_ev + kChunks + r], 0);
+        e = cudaMemcpy2DAsync(j.data + r * w1, n1 * 8, buf + r * w1, n1 * 8, w1 * 8, n2,
+                              cudaMemcpyDeviceToHost, ps->out);
+      }
+      if (e != cudaSuccess) st = gl_cuda_status(e);
+      cudaEventRecord(freed.ev[i], ps->out);
+      continue;
+    }
     if (words_i)
       e = cudaMemcpyAsync(buf, j.data, words_i * 8, cudaMemcpyHostToDevice, ps->in);
     if (e != cudaSuccess) { st = gl_cuda_status(e); break; }
@@ -107,7 +169,7 @@ extern "C" int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_
     for (uint32_t k = 0; k < j.nops && st == GL_OK && words_i; k++) {
       const bool inv = j.dirs[k] == GL_INVERSE;
       if (inv && j.len <= 1) continue;  // ntt/src/ntt/mod.rs:105-107
-      st = gl_enqueue_transform(plans[i], buf, buf, 1, j.count, j.len, inv, scratch, ps->comp);
+      st = gl_enqueue_transform(pl, buf, buf, 1, j.count, j.len, inv, scratch, ps->comp);
     }
     cudaEventRecord(done.ev[i], ps->comp);
     cudaStreamWaitEvent(ps->out, done.ev[i], 0);
@@ -127,6 +189,7 @@ extern "C" int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_
   cudaError_t e2 = cudaStreamSynchronize(ps->out);
   cudaError_t e3 = cudaStreamSynchronize(ps->comp);
   if (last) cudaEventDestroy(last);
+  for (auto ev : chunk_ev) cudaEventDestroy(ev);
   if (st != GL_OK) return st;
   if (e1 != cudaSuccess) return gl_cuda_status(e1);
   if (e2 != cudaSuccess) return gl_cuda_status(e2);

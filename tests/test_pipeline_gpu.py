@@ -33,6 +33,24 @@ def test_pipeline_matches_oracle(gl, oracle, cuda, depth):
         assert np.array_equal(h, want), (n, dirs)
 
 
+def test_pipeline_column_blocks(gl, oracle, cuda):
+    """Large two-pass transforms move in column blocks (2D copies) around the
+    first column pass and the last row pass; 4080 columns split into blocks
+    of 510, not a multiple of the kernel's lanes."""
+    specs = [(1 << 22, ("fwd", "inv")), (3 << 20, ("fwd",)), (16711680, ("inv",)), (1 << 24, ("fwd", "inv", "fwd"))]
+    xs, jobs = [], []
+    for i, (n, dirs) in enumerate(specs):
+        x = gl.fill_uniform(n, seed=0xB10C + i)
+        xs.append(x)
+        jobs.append((pinned(cuda, x) if i != 1 else x.copy(), n, dirs))
+    gl.host_pipeline(jobs)
+    for (h, n, dirs), x in zip(jobs, xs):
+        want = x
+        for d in dirs:
+            want = (oracle.ntt if d == "fwd" else oracle.intt)(want)
+        assert np.array_equal(h, want), (n, dirs)
+
+
 def test_pipeline_errors(gl, cuda):
     x = rand_field(16, seed=1)
     with pytest.raises(ValueError, match="is not a supported NTT size"):
