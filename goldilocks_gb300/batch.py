@@ -21,17 +21,17 @@ AUTO, PERSISTENT, BUCKETS, PER_CALL = (L.GL_BATCH_AUTO, L.GL_BATCH_PERSISTENT, L
 def _polys(items):
     import torch
     arr = (L.Poly * len(items))()
-    stream = None
+    dev = items[0][0].device if isinstance(items[0][0], torch.Tensor) else None
     for i, (t, d) in enumerate(items):
-        if not isinstance(t, torch.Tensor) or not t.is_cuda or t.element_size() != 8:
-            raise TypeError("batch entries must be 64-bit integer CUDA tensors")
+        if not isinstance(t, torch.Tensor) or t.device != dev or not t.is_cuda or t.element_size() != 8:
+            raise TypeError("batch entries must be 64-bit integer tensors on one CUDA device")
         if not t.is_contiguous():
             raise ValueError("batch entries must be contiguous")
-        arr[i].data = t.data_ptr()
-        arr[i].len = t.numel()
-        arr[i].dir = int(d)
-        stream = torch.cuda.current_stream(t.device).cuda_stream
-    return arr, stream
+        p = arr[i]
+        p.data = t.data_ptr()
+        p.len = t.numel()
+        p.dir = d
+    return arr, torch.cuda.current_stream(dev).cuda_stream
 
 
 def run(items, mode=AUTO):

@@ -139,15 +139,24 @@ struct poly_plan {
 
 int resolve(const gl_poly *polys, uint64_t count, std::vector<poly_plan> &out) {
   out.resize(count);
+  // One plan and table lookup per distinct length (the lookups take locks).
+  std::map<uint64_t, std::pair<gl_plan *, gl_dev_tables *>> seen;
   for (uint64_t i = 0; i < count; i++) {
     const gl_poly &p = polys[i];
     if (!p.data && p.len) return GL_ERR_INVALID;
     if (p.dir != GL_FORWARD && p.dir != GL_INVERSE) return GL_ERR_INVALID;
-    int st = gl_plan_create(p.len, &out[i].pl);
-    if (st != GL_OK) return st;
+    auto it = seen.find(p.len);
+    if (it == seen.end()) {
+      gl_plan *pl = nullptr;
+      gl_dev_tables *t = nullptr;
+      int st = gl_plan_create(p.len, &pl);
+      if (st != GL_OK) return st;
+      if (pl->kind > 0 && (st = gl_plan_tables(pl, &t)) != GL_OK) return st;
+      it = seen.emplace(p.len, std::make_pair(pl, t)).first;
+    }
+    out[i].pl = it->second.first;
+    out[i].t = it->second.second;
     out[i].inv = p.dir == GL_INVERSE;
-    out[i].t = nullptr;
-    if (out[i].pl->kind > 0 && (st = gl_plan_tables(out[i].pl, &out[i].t)) != GL_OK) return st;
   }
   return GL_OK;
 }
@@ -312,14 +321,17 @@ int enqueue_persistent(const gl_poly *polys, uint64_t count, const std::vector<p
 
 int run_persistent(const gl_poly *polys, uint64_t count, const std::vector<poly_plan> &pp,
                    cudaStream_t stream) {
-  uint32_t *err = nullptr;
-  cudaError_t e = cudaMallocHost(&err, sizeof(uint32_t));
-  if (e != cudaSuccess) return gl_cuda_status(e);
+  // The kernel's error word comes back through a page-locked word per host
+  // thread, allocated once (pinning memory per call costs more than a batch).
+  thread_local uint32_t *err = nullptr;
+  if (!err) {
+    cudaError_t e = cudaMallocHost(&err, sizeof(uint32_t));
+    if (e != cudaSuccess) { err = nullptr; return gl_cuda_status(e); }
+  }
   *err = 0;
   int st = enqueue_persistent(polys, count, pp, stream, err);
   cudaError_t e2 = cudaStreamSynchronize(stream);
   const uint32_t v = *err;
-  cudaFreeHost(err);
   if (st != GL_OK) return st;
   if (e2 != cudaSuccess) return gl_cuda_status(e2);
   return v ? (int)v : GL_OK;
