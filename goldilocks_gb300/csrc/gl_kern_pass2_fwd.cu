@@ -9,12 +9,6 @@
 static const gl_kernel_entry k_entries[] = {
     GL_ENTRY3M(16, 16, 8, 2, 256, 4, false),
     GL_ENTRY3M(16, 8, 8, 2, 256, 4, false),
-    // Small passes (batches of short transforms): 8-32 lanes fill a
-    // 256-512-thread CTA instead of 32-64 threads with four lanes.
-    GL_ENTRY3M(8, 8, 8, 8, 512, 2, false),
-    GL_ENTRY3M(16, 16, 1, 16, 256, 4, false),
-    GL_ENTRY3M(16, 8, 1, 32, 256, 4, false),
-    GL_ENTRY3M(8, 8, 1, 32, 256, 4, false),
 };
 
 const gl_kernel_entry *gl_kernels_pass2_fwd(size_t *count) {
