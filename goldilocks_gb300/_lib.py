@@ -38,6 +38,9 @@ SIGNATURES = [
     ("gl_convolve", _int, [_vp, _vp, _u64, _u64, _u64, _int, _int, _vp]),
     ("gl_host_pipeline", _int, [_vp, _u64, _u32]),
     ("gl_batch_wait_selftest", _int, [_u64, ctypes.POINTER(_u32)]),
+    ("gl_debug_inject_alloc_failures", _int, [_int]),
+    ("gl_debug_checks_enabled", _int, []),
+    ("gl_debug_check_status", _int, [ctypes.POINTER(_u32)]),
     ("gl_k12_next_layer_size", _u64, [_u64]),
     ("gl_merkle_tree_bytes", _u64, [_u64]),
     ("gl_k12_process_layer", _int, [_vp, _u64, _vp, _int, _vp]),

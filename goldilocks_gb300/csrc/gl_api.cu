@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -563,6 +564,48 @@ extern "C" int gl_profile_read(gl_profile_entry *out, int cap) {
 
 static const uint64_t kMaxGridYZ = 65535;
 
+// Debug builds (-DGL_DEVICE_CHECKS): every pass launch gets the extents of
+// its input and output (in words from its pointers) and the device's check
+// word; gl_debug_check_status reads and clears it.
+#ifdef GL_DEVICE_CHECKS
+static uint32_t *dbg_word() {
+  static std::mutex mu;
+  static std::map<int, uint32_t *> words;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = words.find(dev);
+  if (it == words.end()) {
+    uint32_t *w = nullptr;
+    if (cudaMalloc(&w, sizeof(uint32_t)) != cudaSuccess || cudaMemset(w, 0, sizeof(uint32_t)) != cudaSuccess)
+      return nullptr;
+    it = words.emplace(dev, w).first;
+  }
+  return it->second;
+}
+#define GL_DBG_EXTENTS(args, in_words, out_words) \
+  do { (args).dbg_in_words = (in_words); (args).dbg_out_words = (out_words); (args).dbg_err = dbg_word(); } while (0)
+#else
+#define GL_DBG_EXTENTS(args, in_words, out_words) do {} while (0)
+#endif
+
+extern "C" int gl_debug_checks_enabled(void) { return GL_DBG_CHECKS; }
+
+extern "C" int gl_debug_check_status(uint32_t *flags) {
+  if (!flags) return GL_ERR_INVALID;
+  *flags = 0;
+#ifdef GL_DEVICE_CHECKS
+  uint32_t *w = dbg_word();
+  if (!w) return GL_ERR_CUDA;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(flags, w, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemset(w, 0, sizeof(uint32_t));
+  return gl_cuda_status(e);
+#else
+  return GL_OK;
+#endif
+}
+
 // Queue the transform of a strided batch on `stream`.  Element j of column c
 // of batch item b is at base[b*bs + j*C + c] (C = 1, bs = n: contiguous
 // transforms; C = cols, B = 1: the columns of a row-major matrix).  `src` and
@@ -624,6 +667,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
         a.in = src + off * bs; a.out = dst + off * bs;
         if (om) a.mul = om->factors + off * mul_item;
         a.lanes = (uint32_t)c;
+        GL_DBG_EXTENTS(a, (c - 1) * bs + n, (c - 1) * bs + n);
         gl_launch(k, 0, a, dim3((unsigned)((c + k->lanes - 1) / k->lanes)), c * n, stream);
       }
     } else {
@@ -636,6 +680,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       for (uint64_t off = 0; off < B; off += kMaxGridYZ) {
         const uint64_t c = std::min(kMaxGridYZ, B - off);
         a.in = src + off * bs; a.out = dst + off * bs;
+        GL_DBG_EXTENTS(a, (c - 1) * bs + n * C, (c - 1) * bs + n * C);
         gl_launch(k, 0, a, dim3((unsigned)((C + k->lanes - 1) / k->lanes), (unsigned)c),
                c * n * C, stream);
       }
@@ -667,6 +712,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
         a.flags |= GL_PF_IN_TWIDDLE;
         a.itw_lo = lo->itw_lo; a.itw_hi = lo->itw_hi; a.itw_jmul = n23;
       }
+      GL_DBG_EXTENTS(a, n * C, n * C);
       const uint64_t ta = gl_tiles(n23 * C, ka);
       if (ta > 0x7fffffffull) return GL_ERR_INVALID;
       gl_launch(ka, 1, a, dim3((unsigned)ta), n * C, stream);
@@ -679,6 +725,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       bb.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
       bb.tw_m = bb.tw_r2 = t->blk[1][d]; bb.tw_lo = t->tw23_lo[d]; bb.tw_hi = t->tw23_hi[d];
       bb.tw_lane_div = (uint32_t)C;
+      GL_DBG_EXTENTS(bb, n * C, n * C);
       gl_launch(kb, 1, bb, dim3((unsigned)gl_tiles(n3 * C, kb), (unsigned)n1),
                 n * C, stream);
       gl_pass_args c = base_args();
@@ -686,6 +733,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       c.tw_m = c.tw_r2 = t->blk3[d];
       c.flags = GL_PF_STORE_LANE_FAST;
       c.in = s1; c.out = out;
+      GL_DBG_EXTENTS(c, n * C, n * C);
       if (C == 1) {
         c.in_ls = (int64_t)n3; c.in_is = 1;                       // lanes: rows k2 of block k1
         c.out_ls = (int64_t)n1; c.out_is = (int64_t)(n1 * n2);
@@ -734,6 +782,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       a.flags |= GL_PF_IN_TWIDDLE;
       a.itw_lo = lo->itw_lo; a.itw_hi = lo->itw_hi; a.itw_jmul = n2;
     }
+    GL_DBG_EXTENTS(a, (cb - 1) * bs + n * C, cb * n * C);
     const uint64_t lanes1 = n2 * C;
     if (gl_tiles(lanes1, kc) > 0x7fffffffull) return GL_ERR_INVALID;
     gl_launch(kc, 1, a, dim3((unsigned)gl_tiles(lanes1, kc), (unsigned)cb),
@@ -743,6 +792,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
     b.in_limit = 0xffffffffu;  // zero padding applies to the first pass only
     b.tw_m = b.tw_r2 = t->blk[1][d];
     b.flags = GL_PF_STORE_LANE_FAST;
+    GL_DBG_EXTENTS(b, cb * n * C, (cb - 1) * bs + n * C);
     if (C == 1) {
       b.in = scratch + off * n; b.out = dst + off * bs;
       b.in_ls = (int64_t)n2; b.in_is = 1; b.out_ls = 1; b.out_is = (int64_t)n1;
@@ -794,6 +844,7 @@ int gl_enqueue_pass_range(gl_plan *pl, int stage, const uint64_t *src, uint64_t 
     a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
     a.tw_m = a.tw_r2 = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
     a.tw_col0 = lo;
+    GL_DBG_EXTENTS(a, n1 * n2 - lo, n1 * n2 - lo);
     if (t->tw_full[d]) {
       a.flags |= GL_PF_TW_TABLE;
       a.tw_full = t->tw_full[d];
@@ -807,6 +858,7 @@ int gl_enqueue_pass_range(gl_plan *pl, int stage, const uint64_t *src, uint64_t 
     a.in_ls = (int64_t)n2; a.in_is = 1; a.out_ls = 1; a.out_is = (int64_t)n1;
     a.flags = GL_PF_STORE_LANE_FAST;
     a.tw_m = a.tw_r2 = t->blk[1][d];
+    GL_DBG_EXTENTS(a, n1 * n2 - lo * n2, n1 * n2 - lo);
     gl_launch(kr, 2, a, dim3((unsigned)gl_tiles(hi - lo, kr)), n2 * (hi - lo), stream);
   }
   return gl_cuda_status(cudaGetLastError());
@@ -815,6 +867,24 @@ int gl_enqueue_pass_range(gl_plan *pl, int stage, const uint64_t *src, uint64_t 
 static int run_device(gl_plan *pl, uint64_t *data, uint64_t count, bool inv, uint64_t *scratch,
                       cudaStream_t stream) {
   return gl_enqueue_transform(pl, data, data, 1, count, pl->size, inv, scratch, stream);
+}
+
+static std::atomic<int> g_inject_alloc_failures{0};
+
+cudaError_t gl_malloc_async(void **p, size_t bytes, cudaStream_t stream) {
+  int left = g_inject_alloc_failures.load();
+  while (left > 0) {
+    if (g_inject_alloc_failures.compare_exchange_weak(left, left - 1)) {
+      *p = nullptr;
+      return cudaErrorMemoryAllocation;
+    }
+  }
+  return cudaMallocAsync(p, bytes, stream);
+}
+
+extern "C" int gl_debug_inject_alloc_failures(int count) {
+  g_inject_alloc_failures.store(count > 0 ? count : 0);
+  return GL_OK;
 }
 
 void gl_init_mempool_once() {
@@ -879,7 +949,7 @@ static int execute(gl_plan *pl, uint64_t *data, uint64_t len, int dir, int mem, 
     bool own = false;
     if (need && (!ws || ws_bytes < need)) {
       if (ws) return GL_ERR_INVALID;
-      cudaError_t e = cudaMallocAsync((void **)&scratch, need, stream);
+      cudaError_t e = gl_malloc_async((void **)&scratch, need, stream);
       if (e != cudaSuccess) return gl_cuda_status(e);
       own = true;
     }
@@ -892,7 +962,7 @@ static int execute(gl_plan *pl, uint64_t *data, uint64_t len, int dir, int mem, 
   if (uint64_t *hv = (uint64_t *)gl_host_device_view(data, len * sizeof(uint64_t))) {
     uint64_t *scratch = nullptr;
     if (need) {
-      cudaError_t e = cudaMallocAsync((void **)&scratch, need, stream);
+      cudaError_t e = gl_malloc_async((void **)&scratch, need, stream);
       if (e != cudaSuccess) return gl_cuda_status(e);
     }
     st = run_device(pl, hv, count, inv, scratch, stream);
@@ -902,7 +972,7 @@ static int execute(gl_plan *pl, uint64_t *data, uint64_t len, int dir, int mem, 
   }
   // Host memory: stage through the device and return when the result is back.
   uint64_t *dbuf = nullptr;
-  cudaError_t e = cudaMallocAsync((void **)&dbuf, len * sizeof(uint64_t) + need, stream);
+  cudaError_t e = gl_malloc_async((void **)&dbuf, len * sizeof(uint64_t) + need, stream);
   if (e != cudaSuccess) return gl_cuda_status(e);
   e = cudaMemcpyAsync(dbuf, data, len * sizeof(uint64_t), cudaMemcpyHostToDevice, stream);
   if (e == cudaSuccess) {
@@ -919,12 +989,14 @@ static int execute(gl_plan *pl, uint64_t *data, uint64_t len, int dir, int mem, 
 
 extern "C" int gl_plan_execute(const gl_plan *plan, uint64_t *data, uint64_t len, int dir, int mem,
                                void *stream) {
+  GL_NVTX("gl_plan_execute");
   return execute(const_cast<gl_plan *>(plan), data, len, dir, mem, nullptr, 0,
                  (cudaStream_t)stream);
 }
 
 extern "C" int gl_plan_execute_ws(const gl_plan *plan, uint64_t *data, uint64_t len, int dir,
                                   void *workspace, uint64_t workspace_bytes, void *stream) {
+  GL_NVTX("gl_plan_execute_ws");
   if (!workspace && gl_plan_workspace_bytes(plan, plan && plan->size ? len / plan->size : 0))
     return GL_ERR_INVALID;
   return execute(const_cast<gl_plan *>(plan), data, len, dir, GL_MEM_DEVICE, workspace,
@@ -932,6 +1004,7 @@ extern "C" int gl_plan_execute_ws(const gl_plan *plan, uint64_t *data, uint64_t 
 }
 
 extern "C" int gl_ntt(uint64_t *values, uint64_t len, int mem, void *stream) {
+  GL_NVTX("gl_ntt");
   gl_plan *pl = nullptr;
   int st = gl_plan_create(len, &pl);  // len 0 is not a divisor: the reference panics too
   if (st != GL_OK) return st;
@@ -939,6 +1012,7 @@ extern "C" int gl_ntt(uint64_t *values, uint64_t len, int mem, void *stream) {
 }
 
 extern "C" int gl_intt(uint64_t *values, uint64_t len, int mem, void *stream) {
+  GL_NVTX("gl_intt");
   if (len <= 1) return GL_OK;  // ntt/mod.rs:105-107
   gl_plan *pl = nullptr;
   int st = gl_plan_create(len, &pl);
@@ -955,7 +1029,7 @@ struct gl_tmp {
   int alloc(size_t bytes, cudaStream_t st) {
     s = st;
     if (bytes == 0) return GL_OK;
-    return gl_cuda_status(cudaMallocAsync(&p, bytes, st));
+    return gl_cuda_status(gl_malloc_async((void **)&p, bytes, st));
   }
   ~gl_tmp() { if (p) cudaFreeAsync(p, s); }
   uint64_t *u64() { return (uint64_t *)p; }
@@ -963,6 +1037,7 @@ struct gl_tmp {
 
 extern "C" int gl_ntt_columns(uint64_t *data, uint64_t rows, uint64_t cols, int dir, int mem,
                               void *stream_) {
+  GL_NVTX("gl_ntt_columns");
   cudaStream_t stream = (cudaStream_t)stream_;
   if ((!data && rows * cols) || (dir != GL_FORWARD && dir != GL_INVERSE) ||
       (mem != GL_MEM_HOST && mem != GL_MEM_DEVICE))
@@ -1086,6 +1161,7 @@ int gl_coset_pad(const uint64_t *coef, uint64_t *dst, uint64_t n, uint64_t m, ui
 
 extern "C" int gl_coset_lde(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t cols,
                             uint32_t blowup, uint64_t shift, int mem, void *stream_) {
+  GL_NVTX("gl_coset_lde");
   cudaStream_t stream = (cudaStream_t)stream_;
   if (!in || !out || cols == 0 || blowup == 0) return GL_ERR_INVALID;
   if (mem != GL_MEM_HOST && mem != GL_MEM_DEVICE) return GL_ERR_INVALID;

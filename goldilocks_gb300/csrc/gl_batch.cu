@@ -291,7 +291,7 @@ int enqueue_persistent(const gl_poly *polys, uint64_t count, const std::vector<p
   const size_t o_scr = o_ctr + align(ctr_bytes);
   dev_block blk;
   blk.s = stream;
-  cudaError_t e = cudaMallocAsync(&blk.p, o_scr + scratch_words * 8, stream);
+  cudaError_t e = gl_malloc_async((void **)&blk.p, o_scr + scratch_words * 8, stream);
   if (e != cudaSuccess) return gl_cuda_status(e);
   char *base = (char *)blk.p;
   uint64_t *scratch = (uint64_t *)(base + o_scr);
@@ -375,7 +375,7 @@ int run_buckets(const gl_poly *polys, uint64_t count, const std::vector<poly_pla
     if (pp[order[j]].pl->kind == 2) { scr_off[j] = scratch_words; scratch_words += pp[order[j]].pl->size; }
   dev_block scr;
   scr.s = stream;
-  cudaError_t e = cudaMallocAsync(&scr.p, std::max<uint64_t>(scratch_words, 1) * 8, stream);
+  cudaError_t e = gl_malloc_async((void **)&scr.p, std::max<uint64_t>(scratch_words, 1) * 8, stream);
   if (e != cudaSuccess) return gl_cuda_status(e);
   // Pointer tables: data pointers at [0, n), scratch pointers at [n, 2n).
   const size_t nitems = order.size();
@@ -480,6 +480,7 @@ int gl_batch_enqueue_persistent(const gl_poly *polys, uint64_t count, cudaStream
 }
 
 extern "C" int gl_batch_execute(const gl_poly *polys, uint64_t count, int mode, void *stream_) {
+  GL_NVTX("gl_batch_execute");
   cudaStream_t stream = (cudaStream_t)stream_;
   if (!polys && count) return GL_ERR_INVALID;
   if (count == 0) return GL_OK;

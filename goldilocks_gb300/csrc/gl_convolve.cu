@@ -42,6 +42,7 @@ static int convolve_device(gl_plan *pl, uint64_t *a, const uint64_t *b, uint64_t
 
 extern "C" int gl_convolve(uint64_t *a, const uint64_t *b_hat, uint64_t n, uint64_t count,
                            uint64_t b_count, int repr, int mem, void *stream_) {
+  GL_NVTX("gl_convolve");
   cudaStream_t stream = (cudaStream_t)stream_;
   if (repr != GL_REPR_CANONICAL && repr != GL_REPR_MONTGOMERY) return GL_ERR_INVALID;
   if (mem != GL_MEM_HOST && mem != GL_MEM_DEVICE) return GL_ERR_INVALID;
@@ -59,7 +60,7 @@ extern "C" int gl_convolve(uint64_t *a, const uint64_t *b_hat, uint64_t n, uint6
   if (mem == GL_MEM_DEVICE) {
     uint64_t *scratch = nullptr;
     if (need) {
-      cudaError_t e = cudaMallocAsync((void **)&scratch, need * sizeof(uint64_t), stream);
+      cudaError_t e = gl_malloc_async((void **)&scratch, need * sizeof(uint64_t), stream);
       if (e != cudaSuccess) return gl_cuda_status(e);
     }
     st = convolve_device(pl, a, b_hat, n, count, shared, mont, scratch, stream);
@@ -67,7 +68,7 @@ extern "C" int gl_convolve(uint64_t *a, const uint64_t *b_hat, uint64_t n, uint6
     return st;
   }
   uint64_t *dbuf = nullptr;
-  cudaError_t e = cudaMallocAsync((void **)&dbuf, (len + blen + need) * sizeof(uint64_t), stream);
+  cudaError_t e = gl_malloc_async((void **)&dbuf, (len + blen + need) * sizeof(uint64_t), stream);
   if (e != cudaSuccess) return gl_cuda_status(e);
   e = cudaMemcpyAsync(dbuf, a, len * sizeof(uint64_t), cudaMemcpyHostToDevice, stream);
   if (e == cudaSuccess)

@@ -62,7 +62,7 @@ __device__ __forceinline__ void gl_gen_round1(const gl_pass_args &a, const gl_ge
     for (int t = 0; t < R; t++) {
       const uint32_t j = (uint32_t)(g + q.S1 * t);
       const uint64_t *p = src + (int64_t)(q.S1 * t) * a.in_is;
-      x[t] = (live && j < a.in_limit) ? ((a.flags & GL_PF_LOAD_CG) ? __ldcg(p) : *p) : 0;
+      x[t] = (live && j < a.in_limit) ? gl_ld_in(a, p, (a.flags & GL_PF_LOAD_CG) != 0) : 0;
     }
     if ((a.flags & GL_PF_IN_TWIDDLE) && live) {
       const uint64_t col = (uint64_t)lane / a.tw_lane_div;
@@ -82,7 +82,7 @@ __device__ __forceinline__ void gl_gen_round1(const gl_pass_args &a, const gl_ge
           uint64_t v = scale_all ? gl_mont_mul(x[t], a.tw_m[0]) : x[t];
           if (a.flags & GL_PF_PASS_TWIDDLE) v = gl_mont_mul(v, gl_pass_tw(a, col, t));
           if (a.flags & GL_PF_OUT_MUL) v = gl_out_mul(a, q.mul, lane, t, v);
-          dst[(int64_t)t * a.out_is] = v;
+          gl_st_out(a, dst + (int64_t)t * a.out_is, v);
         }
       }
     } else {
@@ -90,7 +90,7 @@ __device__ __forceinline__ void gl_gen_round1(const gl_pass_args &a, const gl_ge
       for (int t = 0; t < R; t++) {
         uint64_t v = x[t];
         if (t > 0 || scale_all) v = gl_mont_mul(v, __ldg(a.tw_m + g * t));
-        sm[c * q.LS + g + q.S1 * t] = v;
+        gl_sm_st(a, sm, c * q.LS + g + q.S1 * t, GL_GEN_LANES * q.LS, v);
       }
     }
   }
@@ -108,13 +108,13 @@ __device__ __forceinline__ void gl_gen_round2(const gl_pass_args &a, const gl_ge
     const int base = c * q.LS + k1 * q.S1 + d3;
     uint64_t x[R];
 #pragma unroll
-    for (int t = 0; t < R; t++) x[t] = sm[base + q.R3 * t];
+    for (int t = 0; t < R; t++) x[t] = gl_sm_ld(a, sm, base + q.R3 * t, GL_GEN_LANES * q.LS);
     gl_dft<R, INV>(x);
 #pragma unroll
     for (int t = 0; t < R; t++) {
       uint64_t v = x[t];
       if (t > 0) v = gl_mont_mul(v, __ldg(a.tw_r2 + q.R1 * d3 * t));
-      sm[base + q.R3 * t] = v;
+      gl_sm_st(a, sm, base + q.R3 * t, GL_GEN_LANES * q.LS, v);
     }
   }
 }
@@ -140,7 +140,7 @@ __device__ __forceinline__ void gl_gen_round_last(const gl_pass_args &a, const g
     }
     uint64_t x[R];
 #pragma unroll
-    for (int t = 0; t < R; t++) x[t] = sm[c * q.LS + base + t];
+    for (int t = 0; t < R; t++) x[t] = gl_sm_ld(a, sm, c * q.LS + base + t, GL_GEN_LANES * q.LS);
     gl_dft<R, INV>(x);
     const int64_t lane = q.lane0 + c;
     if (lane < (int64_t)a.lanes) {
@@ -152,7 +152,7 @@ __device__ __forceinline__ void gl_gen_round_last(const gl_pass_args &a, const g
         uint64_t v = x[t];
         if (a.flags & GL_PF_PASS_TWIDDLE) v = gl_mont_mul(v, gl_pass_tw(a, col, k));
         if (a.flags & GL_PF_OUT_MUL) v = gl_out_mul(a, q.mul, lane, (int64_t)k, v);
-        dst[(int64_t)k * a.out_is] = v;
+        gl_st_out(a, dst + (int64_t)k * a.out_is, v);
       }
     }
   }

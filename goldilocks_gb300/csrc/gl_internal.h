@@ -9,8 +9,23 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/goldilocks_gpu.h"
 #include "gl_pass3.cuh"
+
+// NVTX range over a public entry point (visible in Nsight timelines; a no-op
+// when no tool is attached).
+struct gl_nvtx_range {
+  explicit gl_nvtx_range(const char *name) { nvtxRangePushA(name); }
+  ~gl_nvtx_range() { nvtxRangePop(); }
+};
+#define GL_NVTX(name) gl_nvtx_range gl_nvtx_scope_(name)
+
+// Stream-ordered allocation of a call's temporaries.  Failures can be
+// injected on the host (gl_debug_inject_alloc_failures) to test that
+// GL_ERR_OOM propagates without touching the caller's data.  (gl_api.cu)
+cudaError_t gl_malloc_async(void **p, size_t bytes, cudaStream_t stream);
 
 typedef void (*gl_launch_fn)(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
 

@@ -121,7 +121,7 @@ static int staged(const void *in, uint64_t in_bytes, void *out, uint64_t out_byt
                   F body) {
   gl_init_mempool_once();
   uint8_t *d = nullptr;
-  cudaError_t e = cudaMallocAsync((void **)&d, in_bytes + out_bytes + 16, stream);
+  cudaError_t e = gl_malloc_async((void **)&d, in_bytes + out_bytes + 16, stream);
   if (e != cudaSuccess) return gl_cuda_status(e);
   uint8_t *dout = d + ((in_bytes + 15) / 16) * 16;  // 16-byte aligned output
   int st = GL_OK;
@@ -140,6 +140,7 @@ static int staged(const void *in, uint64_t in_bytes, void *out, uint64_t out_byt
 
 extern "C" int gl_k12_process_layer(const uint8_t *in, uint64_t len, uint8_t *out, int mem,
                                     void *stream_) {
+  GL_NVTX("gl_k12_process_layer");
   cudaStream_t stream = (cudaStream_t)stream_;
   if ((mem != GL_MEM_HOST && mem != GL_MEM_DEVICE) || (len && (!in || !out))) return GL_ERR_INVALID;
   if (mem == GL_MEM_DEVICE) return layer_device(in, len, out, stream);
@@ -149,6 +150,7 @@ extern "C" int gl_k12_process_layer(const uint8_t *in, uint64_t len, uint8_t *ou
 
 extern "C" int gl_k12_hash_many(const uint8_t *in, uint64_t msg_len, uint64_t count, uint8_t *out,
                                 uint32_t out_len, int mem, void *stream_) {
+  GL_NVTX("gl_k12_hash_many");
   cudaStream_t stream = (cudaStream_t)stream_;
   if (msg_len > 166 || out_len > 168 || (mem != GL_MEM_HOST && mem != GL_MEM_DEVICE)) return GL_ERR_INVALID;
   if (count == 0 || out_len == 0) return GL_OK;
@@ -178,6 +180,7 @@ static int merkle_device(const uint8_t *values, uint64_t len, uint8_t *layers, c
 
 extern "C" int gl_merkle_tree(const uint8_t *values, uint64_t len, uint8_t *layers, uint64_t layers_bytes,
                               int mem, void *stream_) {
+  GL_NVTX("gl_merkle_tree");
   cudaStream_t stream = (cudaStream_t)stream_;
   if (mem != GL_MEM_HOST && mem != GL_MEM_DEVICE) return GL_ERR_INVALID;
   const uint64_t need = gl_merkle_tree_bytes(len);
@@ -200,6 +203,7 @@ static ulonglong4 challenge_lanes(const uint8_t *challenge) {
 
 extern "C" int gl_pow_hashes(const uint8_t *challenge, uint64_t start, uint64_t count, uint64_t *out,
                              int mem, void *stream_) {
+  GL_NVTX("gl_pow_hashes");
   cudaStream_t stream = (cudaStream_t)stream_;
   if (!challenge || (mem != GL_MEM_HOST && mem != GL_MEM_DEVICE)) return GL_ERR_INVALID;
   if (count == 0) return GL_OK;
@@ -225,13 +229,14 @@ extern "C" int gl_pow_verify(const uint8_t *challenge, uint64_t threshold, uint6
 
 extern "C" int gl_pow_solve(const uint8_t *challenge, uint64_t threshold, uint64_t start,
                             uint64_t max_count, uint64_t *nonce, void *stream_) {
+  GL_NVTX("gl_pow_solve");
   cudaStream_t stream = (cudaStream_t)stream_;
   if (!challenge || !nonce) return GL_ERR_INVALID;
   if (max_count > UINT64_MAX - start) max_count = UINT64_MAX - start;  // nonces stay below 2^64 - 1
   const ulonglong4 c = challenge_lanes(challenge);
   gl_init_mempool_once();
   unsigned long long *best = nullptr;
-  cudaError_t e = cudaMallocAsync((void **)&best, sizeof(*best), stream);
+  cudaError_t e = gl_malloc_async((void **)&best, sizeof(*best), stream);
   if (e != cudaSuccess) return gl_cuda_status(e);
   int st = gl_cuda_status(cudaMemsetAsync(best, 0xff, sizeof(*best), stream));
   unsigned long long found = ~0ull;

@@ -83,6 +83,7 @@ uint64_t root_of(uint64_t order, bool inv) {
 }  // namespace
 
 extern "C" int gl_ntt_noalloc(uint64_t *data, uint64_t len, int dir, void *stream_) {
+  GL_NVTX("gl_ntt_noalloc");
   cudaStream_t stream = (cudaStream_t)stream_;
   if (!data || (dir != GL_FORWARD && dir != GL_INVERSE)) return GL_ERR_INVALID;
   if (!gl_is_divisor(len)) return GL_ERR_UNSUPPORTED_SIZE;

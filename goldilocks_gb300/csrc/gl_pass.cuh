@@ -57,11 +57,49 @@ struct gl_pass_args {
   uint64_t *const *out_ptrs;
   int32_t gen_r[3];                 // run-time radices of gl_generic_kernel
   uint64_t tw_col0;                 // pass twiddle column of lane 0 (a launch over a lane range)
+  // Debug builds (-DGL_DEVICE_CHECKS): extents, in words from `in` / `out`,
+  // that every global access must stay within (0: unchecked), and the word
+  // that collects GL_DBG_* bits of violations.
+  uint64_t dbg_in_words, dbg_out_words;
+  uint32_t *dbg_err;
   // GL_PF_OUT_MUL: the factor of output k of lane `lane` in batch item (by, bz)
   // is mul[by*mul_bs + bz*mul_bs2 + lane*mul_ls + k*out_is].
   const uint64_t *mul;
   int64_t mul_ls, mul_bs, mul_bs2;
 };
+
+// Debug builds check every global and shared-memory index the pass kernels
+// use against its extent; a violation sets a bit of *dbg_err and the access
+// is skipped, so nothing traps.  Normal builds compile the checks away.
+#ifdef GL_DEVICE_CHECKS
+#define GL_DBG_CHECKS 1
+#else
+#define GL_DBG_CHECKS 0
+#endif
+enum : uint32_t { GL_DBG_IN = 1u, GL_DBG_OUT = 2u, GL_DBG_SMEM = 4u };
+
+__device__ __forceinline__ bool gl_dbg_ok(const gl_pass_args &a, int64_t off, uint64_t lim,
+                                          uint32_t bit) {
+  if (!GL_DBG_CHECKS || lim == 0 || (off >= 0 && (uint64_t)off < lim)) return true;
+  if (a.dbg_err) atomicOr(a.dbg_err, bit);
+  return false;
+}
+
+// Global load / store of a pass kernel (checked in debug builds).
+__device__ __forceinline__ uint64_t gl_ld_in(const gl_pass_args &a, const uint64_t *p, bool cg) {
+  if (!gl_dbg_ok(a, p - a.in, a.dbg_in_words, GL_DBG_IN)) return 0;
+  return cg ? __ldcg(p) : *p;
+}
+__device__ __forceinline__ void gl_st_out(const gl_pass_args &a, uint64_t *p, uint64_t v) {
+  if (gl_dbg_ok(a, p - a.out, a.dbg_out_words, GL_DBG_OUT)) *p = v;
+}
+// Shared-memory word i of a tile of `lim` words.
+__device__ __forceinline__ uint64_t gl_sm_ld(const gl_pass_args &a, const uint64_t *sm, int i, int lim) {
+  return gl_dbg_ok(a, i, (uint64_t)lim, GL_DBG_SMEM) ? sm[i] : 0;
+}
+__device__ __forceinline__ void gl_sm_st(const gl_pass_args &a, uint64_t *sm, int i, int lim, uint64_t v) {
+  if (gl_dbg_ok(a, i, (uint64_t)lim, GL_DBG_SMEM)) sm[i] = v;
+}
 
 // Every table a pass kernel multiplies by (tw_m, tw_r2, tw_lo/hi, tw_full,
 // itw_lo/hi) holds Montgomery forms t*2^64 mod p, and the kernels multiply

@@ -73,13 +73,13 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
 #pragma unroll
         for (int t = 0; t < R1; t++) {
           const uint32_t j = (uint32_t)(g + S1 * t);
-          x[t] = (live && j < a.in_limit) ? __ldcg(src + (int64_t)(S1 * t) * a.in_is) : 0;
+          x[t] = (live && j < a.in_limit) ? gl_ld_in(a, src + (int64_t)(S1 * t) * a.in_is, true) : 0;
         }
       } else {
 #pragma unroll
         for (int t = 0; t < R1; t++) {
           const uint32_t j = (uint32_t)(g + S1 * t);
-          x[t] = (live && j < a.in_limit) ? src[(int64_t)(S1 * t) * a.in_is] : 0;
+          x[t] = (live && j < a.in_limit) ? gl_ld_in(a, src + (int64_t)(S1 * t) * a.in_is, false) : 0;
         }
       }
       if (a.flags & GL_PF_IN_TWIDDLE) {
@@ -104,14 +104,14 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
             const uint64_t col = (uint64_t)lane / a.tw_lane_div;
 #pragma unroll
             for (int t = 0; t < R1; t++)
-              dst[(int64_t)t * a.out_is] = gl_mont_mul(x[t], gl_pass_tw(a, col, t));
+              gl_st_out(a, dst + (int64_t)t * a.out_is, gl_mont_mul(x[t], gl_pass_tw(a, col, t)));
           } else if (a.flags & GL_PF_OUT_MUL) {
             const uint64_t *mb = a.mul + by * a.mul_bs + bz * a.mul_bs2;
 #pragma unroll
-            for (int t = 0; t < R1; t++) dst[(int64_t)t * a.out_is] = gl_out_mul(a, mb, lane, t, x[t]);
+            for (int t = 0; t < R1; t++) gl_st_out(a, dst + (int64_t)t * a.out_is, gl_out_mul(a, mb, lane, t, x[t]));
           } else {
 #pragma unroll
-            for (int t = 0; t < R1; t++) dst[(int64_t)t * a.out_is] = x[t];
+            for (int t = 0; t < R1; t++) gl_st_out(a, dst + (int64_t)t * a.out_is, x[t]);
           }
         }
       } else {
@@ -119,7 +119,7 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
         for (int t = 0; t < R1; t++) {
           uint64_t v = x[t];
           if (t > 0 || scale_all) v = gl_mont_mul(v, __ldg(a.tw_m + g * t));
-          sm[L::word(c, g + S1 * t)] = v;
+          gl_sm_st(a, sm, L::word(c, g + S1 * t), LANES * L::LS, v);
         }
       }
     }
@@ -136,13 +136,13 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
       const int base = k1 * S1 + d3;
       uint64_t x[R2];
 #pragma unroll
-      for (int t = 0; t < R2; t++) x[t] = sm[L::word(c, base + R3 * t)];
+      for (int t = 0; t < R2; t++) x[t] = gl_sm_ld(a, sm, L::word(c, base + R3 * t), LANES * L::LS);
       gl_dft<R2, INV>(x);
 #pragma unroll
       for (int t = 0; t < R2; t++) {
         uint64_t v = x[t];
         if (t > 0) v = gl_mont_mul(v, __ldg(a.tw_r2 + R1 * d3 * t));
-        sm[L::word(c, base + R3 * t)] = v;
+        gl_sm_st(a, sm, L::word(c, base + R3 * t), LANES * L::LS, v);
       }
     }
     __syncthreads();
@@ -170,7 +170,7 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
       }
       uint64_t x[RL];
 #pragma unroll
-      for (int t = 0; t < RL; t++) x[t] = sm[L::word(c, base + t)];
+      for (int t = 0; t < RL; t++) x[t] = gl_sm_ld(a, sm, L::word(c, base + t), LANES * L::LS);
       gl_dft<RL, INV>(x);
       const int64_t lane = lane0 + c;
       if (lane < (int64_t)a.lanes) {
@@ -180,16 +180,16 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
 #pragma unroll
           for (int t = 0; t < RL; t++) {
             const uint64_t k = (uint64_t)(kbase + SL * t);
-            dst[(int64_t)k * a.out_is] = gl_mont_mul(x[t], gl_pass_tw(a, col, k));
+            gl_st_out(a, dst + (int64_t)k * a.out_is, gl_mont_mul(x[t], gl_pass_tw(a, col, k)));
           }
         } else if (a.flags & GL_PF_OUT_MUL) {
           const uint64_t *mb = a.mul + by * a.mul_bs + bz * a.mul_bs2;
 #pragma unroll
           for (int t = 0; t < RL; t++)
-            dst[(int64_t)(kbase + SL * t) * a.out_is] = gl_out_mul(a, mb, lane, kbase + SL * t, x[t]);
+            gl_st_out(a, dst + (int64_t)(kbase + SL * t) * a.out_is, gl_out_mul(a, mb, lane, kbase + SL * t, x[t]));
         } else {
 #pragma unroll
-          for (int t = 0; t < RL; t++) dst[(int64_t)(kbase + SL * t) * a.out_is] = x[t];
+          for (int t = 0; t < RL; t++) gl_st_out(a, dst + (int64_t)(kbase + SL * t) * a.out_is, x[t]);
         }
       }
     }

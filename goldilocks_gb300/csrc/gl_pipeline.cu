@@ -63,6 +63,7 @@ struct events {
 }  // namespace
 
 extern "C" int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_t depth) {
+  GL_NVTX("gl_host_pipeline");
   if (njobs == 0) return GL_OK;
   if (!jobs) return GL_ERR_INVALID;
   if (depth == 0) depth = 3;
@@ -89,7 +90,7 @@ extern "C" int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_
   gl_init_mempool_once();
   uint64_t *block = nullptr;
   const uint64_t words = depth * slot_words + scratch_words;
-  cudaError_t e = cudaMallocAsync((void **)&block, std::max<uint64_t>(words, 1) * 8, ps->comp);
+  cudaError_t e = gl_malloc_async((void **)&block, std::max<uint64_t>(words, 1) * 8, ps->comp);
   if (e != cudaSuccess) return gl_cuda_status(e);
   events ready, done, freed, alloc;
   if ((st = ready.make(njobs)) != GL_OK || (st = done.make(njobs)) != GL_OK ||

@@ -255,6 +255,7 @@ extern "C" int gl_server_request_bytes(const gl_request *req, uint64_t *bytes) {
 }
 
 extern "C" int gl_server_submit(gl_server *s, const gl_request *req, uint64_t *id) {
+  GL_NVTX("gl_server_submit");
   if (!s || !req || !id) return GL_ERR_INVALID;
   uint64_t bytes = 0;
   int st = footprint(*req, &bytes);

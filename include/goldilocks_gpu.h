@@ -223,6 +223,21 @@ int gl_batch_execute(const gl_poly *polys, uint64_t count, int mode, void *strea
  * The polynomials are transformed (1 + reps) times per mode. */
 int gl_batch_autotune(const gl_poly *polys, uint64_t count, int reps, void *stream, double *ms_out);
 
+/* Fault injection on the host: the next `count` device allocations the
+ * library makes for a call's temporaries (scratch, staging, batch blocks)
+ * fail as if the GPU were out of memory, so that tests can check that
+ * GL_ERR_OOM comes back and the caller's data is untouched.  0 clears it. */
+int gl_debug_inject_alloc_failures(int count);
+
+/* Debug builds (compiled with -DGL_DEVICE_CHECKS): the pass kernels check
+ * every global and shared-memory index against the extents of their buffers;
+ * a violation skips the access and sets a bit (1 input, 2 output, 4 shared
+ * memory) in a per-device word.  gl_debug_checks_enabled() says whether this
+ * build checks; gl_debug_check_status synchronises the device, returns the
+ * bits in *flags and clears them (always 0 in normal builds). */
+int gl_debug_checks_enabled(void);
+int gl_debug_check_status(uint32_t *flags);
+
 /* Diagnostic for the persistent kernel's bounded waits: runs it on one work
  * item whose dependency is never satisfied, with the wait limited to wait_ns
  * (clamped to 1 ms .. 2 s); *status receives the kernel's error word, which

@@ -40,6 +40,24 @@ def cuda():
     return torch
 
 
+@pytest.fixture(autouse=True)
+def _device_index_checks(request):
+    """Under a debug build of the library (-DGL_DEVICE_CHECKS, selected with
+    GOLDILOCKS_BUILD_DIR / GOLDILOCKS_NVCC_FLAGS), every GPU test must leave
+    the device-side index checks clean."""
+    yield
+    if request.node.get_closest_marker("gpu") is None:
+        return
+    import ctypes
+    from goldilocks_gb300 import _lib as L
+    lib = L.load()
+    if not lib.gl_debug_checks_enabled():
+        return
+    flags = ctypes.c_uint32(0)
+    assert lib.gl_debug_check_status(ctypes.byref(flags)) == L.GL_OK
+    assert flags.value == 0, "device index check failed (bits %d)" % flags.value
+
+
 def rand_field(n, seed):
     rng = np.random.default_rng(seed)
     x = rng.integers(0, 2**63, size=n, dtype=np.uint64) * np.uint64(2) + rng.integers(0, 2, size=n, dtype=np.uint64)

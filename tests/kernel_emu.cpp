@@ -29,6 +29,11 @@ static std::barrier<> *g_bar = nullptr;
 
 uint64_t sm[1 << 16];  // the CTA's dynamic shared memory
 
+// Debug-check plumbing (the kernels' GL_DEVICE_CHECKS branch, when compiled in).
+#define atomicOr(p, v) __atomic_fetch_or((p), (v), __ATOMIC_RELAXED)
+static uint64_t g_dbg_in = 0, g_dbg_out = 0;
+static uint32_t g_dbg_err = 0;
+
 #include "gl_pass3.cuh"
 #include "gl_generic.cuh"
 
@@ -84,6 +89,7 @@ int emu_generic(EMU_ARGS) {
   a.lanes = lanes; a.flags = flags; a.tw_m = tw_m; a.tw_r2 = tw_r2; a.tw_lo = tw_lo; a.tw_hi = tw_hi;
   a.tw_lane_div = tw_lane_div; a.in_limit = in_limit;
   a.itw_lo = itw_lo; a.itw_hi = itw_hi; a.itw_jmul = itw_jmul;
+  a.dbg_in_words = g_dbg_in; a.dbg_out_words = g_dbg_out; a.dbg_err = &g_dbg_err;
   a.gen_r[0] = r1; a.gen_r[1] = r2; a.gen_r[2] = r3;
   const unsigned gx = (lanes + GL_GEN_LANES - 1) / GL_GEN_LANES;
   if (inv) run_generic<true>(a, gx);
@@ -99,6 +105,7 @@ int emu_pass3(EMU_ARGS) {
   a.lanes = lanes; a.flags = flags; a.tw_m = tw_m; a.tw_r2 = tw_r2; a.tw_lo = tw_lo; a.tw_hi = tw_hi;
   a.tw_lane_div = tw_lane_div; a.in_limit = in_limit;
   a.itw_lo = itw_lo; a.itw_hi = itw_hi; a.itw_jmul = itw_jmul;
+  a.dbg_in_words = g_dbg_in; a.dbg_out_words = g_dbg_out; a.dbg_err = &g_dbg_err;
   const unsigned gx = (lanes + 3) / 4;
 #define SHAPE(R1, R2, R3, NT)                                                        \
   if (r1 == R1 && r2 == R2 && r3 == R3) {                                              \
@@ -112,5 +119,18 @@ int emu_pass3(EMU_ARGS) {
   SHAPE(16, 8, 8, 512)
   SHAPE(16, 16, 8, 1024)
   return -1;
+}
+
+// Extents (in words) for the next emulated launches; 0 leaves them unchecked.
+void emu_set_checks(uint64_t in_words, uint64_t out_words) {
+  g_dbg_in = in_words;
+  g_dbg_out = out_words;
+}
+
+// GL_DBG_* bits of the violations since the last call, then cleared.
+uint32_t emu_check_flags() {
+  const uint32_t f = g_dbg_err;
+  g_dbg_err = 0;
+  return f;
 }
 }

@@ -71,3 +71,38 @@ def test_bounded_wait_reports_timeout_and_context_survives(gl, oracle, cuda):
     d = cuda.tensor(x.view(np.int64), device="cuda")
     gl.ntt(d)
     assert np.array_equal(d.cpu().numpy().view(np.uint64), oracle.ntt(x))
+
+
+def test_injected_allocation_failures_propagate(gl, cuda):
+    """An allocation refused on the host side (injected) comes back as
+    GL_ERR_OOM from every kind of call, leaves the data untouched, and the
+    next call succeeds."""
+    from goldilocks_gb300 import batch as B
+    L = gl._lib
+    lib = L.load()
+    x = gl.fill_uniform(1 << 16, seed=4)
+    d = cuda.tensor(x.view(np.int64), device="cuda")
+    s = cuda.cuda.current_stream().cuda_stream
+    try:
+        lib.gl_debug_inject_alloc_failures(1)
+        with pytest.raises(gl.GoldilocksError) as e:      # two-pass plan: scratch
+            gl.ntt(d)
+        assert e.value.status == L.GL_ERR_OOM
+        assert np.array_equal(d.cpu().numpy().view(np.uint64), x)
+        lib.gl_debug_inject_alloc_failures(1)
+        h = x.copy()                                      # pageable host memory: staging
+        with pytest.raises(gl.GoldilocksError) as e:
+            gl.ntt(h)
+        assert e.value.status == L.GL_ERR_OOM and np.array_equal(h, x)
+        lib.gl_debug_inject_alloc_failures(1)
+        assert lib.gl_ntt_columns(d.data_ptr(), 1 << 13, 8, L.GL_FORWARD, L.GL_MEM_DEVICE, s) == L.GL_ERR_OOM
+        lib.gl_debug_inject_alloc_failures(1)
+        with pytest.raises(gl.GoldilocksError) as e:
+            B.run([(d, B.FORWARD)], mode=B.BUCKETS)
+        assert e.value.status == L.GL_ERR_OOM
+        assert np.array_equal(d.cpu().numpy().view(np.uint64), x)
+    finally:
+        lib.gl_debug_inject_alloc_failures(0)
+    gl.ntt(d)                                             # and the library keeps working
+    gl.intt(d)
+    assert np.array_equal(d.cpu().numpy().view(np.uint64), x)

@@ -17,18 +17,30 @@ F_PASS_TW, F_SCALE, F_LOAD_LF, F_STORE_LF, F_IN_TW = 1, 2, 4, 8, 16
 NOLIM = 0xFFFFFFFF
 
 
-@pytest.fixture(scope="module")
-def emu(tmp_path_factory):
+def build_emu(tmp_path_factory, extra=()):
     so = tmp_path_factory.mktemp("emu") / "emu.so"
-    subprocess.run(["g++", "-std=c++20", "-O1", "-fPIC", "-shared", "-pthread",
+    subprocess.run(["g++", "-std=c++20", "-O1", "-fPIC", "-shared", "-pthread", *extra,
                     "-I" + os.path.join(ROOT, "goldilocks_gb300", "csrc"),
                     os.path.join(HERE, "kernel_emu.cpp"), "-o", str(so)], check=True)
     lib = ctypes.CDLL(str(so))
+    lib.emu_set_checks.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+    lib.emu_check_flags.restype = ctypes.c_uint32
     vp, i64, u32, u64 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint64
     for f in (lib.emu_pass3, lib.emu_generic):
         f.argtypes = [ctypes.c_int] * 4 + [vp, vp, i64, i64, i64, i64, u32, u32,
                                            vp, vp, vp, vp, u32, u32, vp, vp, u64]
     return lib
+
+
+@pytest.fixture(scope="module")
+def emu(tmp_path_factory):
+    return build_emu(tmp_path_factory)
+
+
+@pytest.fixture(scope="module")
+def emu_checked(tmp_path_factory):
+    """The kernels of a debug build (-DGL_DEVICE_CHECKS)."""
+    return build_emu(tmp_path_factory, ("-DGL_DEVICE_CHECKS",))
 
 
 def root(n, inv=False):
@@ -127,3 +139,38 @@ def test_four_step_zero_padded_coset(emu, oracle):
     full = np.zeros(n1 * n2, dtype=np.uint64)
     full[:rows] = [int(c) * pow(g, j, P) % P for j, c in enumerate(coeffs)]
     assert np.array_equal(got, oracle.ntt(full))
+
+
+@pytest.mark.parametrize("shape", [(16, 16, 1), (8, 8, 8), ("gen", 17, 15, 1)])
+def test_debug_checks_clean_on_exact_extents(emu_checked, oracle, shape):
+    """A debug build's index checks stay silent when every access is in range
+    (whole transforms and a four-step column + row pass)."""
+    r = shape[1:] if shape[0] == "gen" else shape
+    m, cols = r[0] * r[1] * r[2], 5
+    x = rand_field(m * cols, seed=m)
+    out = np.zeros_like(x)
+    emu_checked.emu_set_checks(x.size, out.size)
+    tw = table(root(m), m)
+    call(emu_checked, shape, False, x, out, 1, cols, 1, cols, cols, F_LOAD_LF | F_STORE_LF, tw, tw)
+    assert emu_checked.emu_check_flags() == 0
+    want = np.stack([oracle.ntt(x.reshape(m, cols)[:, c].copy()) for c in range(cols)], axis=1)
+    assert np.array_equal(out.reshape(m, cols), want)
+    emu_checked.emu_set_checks(64 * 512, 64 * 512)
+    x2 = rand_field(64 * 512, seed=3)
+    assert np.array_equal(four_step(emu_checked, 64, 512, (8, 8, 1), (8, 8, 8), x2), oracle.ntt(x2))
+    assert emu_checked.emu_check_flags() == 0
+    emu_checked.emu_set_checks(0, 0)
+
+
+def test_debug_checks_flag_and_skip_out_of_range(emu_checked):
+    """A mistake planted on the CPU: the input extent one column short.  The
+    check flags it (bit 1, input) and skips the access instead of reading
+    past the buffer; outputs stay in range."""
+    m, cols = 64, 4
+    x = rand_field(m * cols - 1, seed=5)         # one word short of m x cols
+    out = np.zeros(m * cols, dtype=np.uint64)
+    emu_checked.emu_set_checks(x.size, out.size)
+    tw = table(root(m), m)
+    call(emu_checked, (8, 8, 1), False, x, out, 1, cols, 1, cols, cols, F_LOAD_LF | F_STORE_LF, tw, tw)
+    assert emu_checked.emu_check_flags() == 1
+    emu_checked.emu_set_checks(0, 0)
