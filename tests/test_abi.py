@@ -40,7 +40,7 @@ def test_divisors_split_next(gl, oracle):
 
 
 def test_plan_describe_matches_reference_tree(gl, oracle):
-    for n in (2, 64, 4096, 1 << 16, 1 << 24, 16711680, 1020):
+    for n in (2, 64, 4096, 1 << 16, 1 << 24, 16711680, 1020, 257, 257 * 16, 65537, 65537 * 3, 257 * 65537):
         try:
             pl = gl.strategy(n)
         except ValueError:
