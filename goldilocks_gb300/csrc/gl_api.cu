@@ -194,6 +194,15 @@ const gl_kernel_entry *gl_find_kernel(uint64_t m, bool full, bool inv) {
   return gl_find_kernel4(m, inv);
 }
 
+const gl_kernel_entry *gl_find_kernel_cols(uint64_t m, bool inv) {
+  size_t cnt = 0;
+  if (use_two_lane_passes()) {  // GOLDILOCKS_PASS_LANES=4 keeps four lanes here too
+    const gl_kernel_entry *e = inv ? gl_kernels_cols_inv(&cnt) : gl_kernels_cols_fwd(&cnt);
+    if (const gl_kernel_entry *k = find_in(e, cnt, m)) return k;
+  }
+  return gl_find_kernel4(m, inv);
+}
+
 const gl_kernel_entry *gl_find_kernel4(uint64_t m, bool inv) {
   size_t cnt = 0;
   if (use_wide_kernels()) {
@@ -253,8 +262,8 @@ static void choose_schedule(gl_plan *pl) {
     for (int d = 0; d < 2; d++) {
       pl->k[0][d] = gl_find_kernel(pl->n1, false, d == 1);
       pl->k[1][d] = gl_find_kernel(pl->n2, false, d == 1);
-      pl->k4[0][d] = gl_find_kernel4(pl->n1, d == 1);
-      pl->k4[1][d] = gl_find_kernel4(pl->n2, d == 1);
+      pl->k4[0][d] = gl_find_kernel_cols(pl->n1, d == 1);
+      pl->k4[1][d] = gl_find_kernel_cols(pl->n2, d == 1);
     }
     return;
   }
@@ -286,7 +295,7 @@ static void choose_schedule(gl_plan *pl) {
       pl->k[1][d] = gl_find_kernel(pl->n2, false, d == 1);
       pl->k[2][d] = gl_find_kernel(pl->n3, false, d == 1);
       for (int s = 0; s < 3; s++)
-        pl->k4[s][d] = gl_find_kernel4(s == 0 ? pl->n1 : s == 1 ? pl->n2 : pl->n3, d == 1);
+        pl->k4[s][d] = gl_find_kernel_cols(s == 0 ? pl->n1 : s == 1 ? pl->n2 : pl->n3, d == 1);
     }
     return;
   }

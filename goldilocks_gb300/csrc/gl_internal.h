@@ -68,6 +68,10 @@ inline uint64_t gl_tiles(uint64_t lanes, const gl_kernel_entry *k) { return (lan
 const gl_kernel_entry *gl_find_kernel(uint64_t m, bool full, bool inv);
 // The pass kernel for m with four lanes per CTA (or the run-time-radix one).
 const gl_kernel_entry *gl_find_kernel4(uint64_t m, bool inv);
+// The pass kernel for m over interleaved columns (C > 1).
+const gl_kernel_entry *gl_find_kernel_cols(uint64_t m, bool inv);
+const gl_kernel_entry *gl_kernels_cols_fwd(size_t *count);
+const gl_kernel_entry *gl_kernels_cols_inv(size_t *count);
 
 #define GL_PASS_LANES 4  // pass sizes are multiples of it; every pass kernel's lanes divide it
 #define GL_TW_SPLIT 4096  // two-level pass twiddle: e = hi*4096 + lo
@@ -88,6 +92,7 @@ struct gl_dev_tables {
   // (the inverse one scaled by 1/q).
   uint64_t *rader_bhat[2] = {nullptr, nullptr};
   uint32_t *rader_gpow = nullptr, *rader_gneg = nullptr;
+  uint32_t *rader_kpos = nullptr;  // kpos[k] = p with g^-p = k (k >= 1)
   uint64_t *rader_tw_lo[2] = {nullptr, nullptr};
   uint64_t *rader_tw_hi[2] = {nullptr, nullptr};
   std::vector<void *> owned;
@@ -103,8 +108,9 @@ struct gl_plan {
   gl_plan *pq = nullptr;    // kind 4: plan of q - 1 (the cyclic convolution)
   gl_plan *pm = nullptr;    // kind 4: plan of m = size / q (may itself be kind 4)
   const gl_kernel_entry *k[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};  // [stage][dir]
-  // The same stages with four-lane kernels, for interleaved columns (C > 1):
-  // there a two-lane CTA reads and writes 16-byte row pieces.
+  // The same stages for interleaved columns (C > 1): four lanes or more per
+  // CTA (a two-lane CTA would read and write 16-byte row pieces), 8-32 lanes
+  // for passes up to 512 points.
   const gl_kernel_entry *k4[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
   std::string tree;
   std::mutex mu;

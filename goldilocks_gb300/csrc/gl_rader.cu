@@ -101,6 +101,31 @@ __global__ void gl_rader_scatter_kernel(const uint64_t *conv, const uint64_t *x0
   }
 }
 
+// The same scatter for few columns (C < 8), where the direct one writes
+// words q*C apart: a 32 x 32 tile of (k1, l) read row by row (rows k1 in the
+// order of the output, each the contiguous row kpos[k1] of conv) and written
+// out along k1, so that both sides move 256-byte runs.
+__global__ void __launch_bounds__(256) gl_rader_scatter_tiled_kernel(
+    const uint64_t *conv, const uint64_t *x0, const uint64_t *X0, uint64_t *Y, const uint32_t *kpos,
+    const uint64_t *tw_lo, const uint64_t *tw_hi, uint64_t C, uint64_t L, uint32_t q) {
+  __shared__ uint64_t tile[32][33];
+  const uint64_t l0 = (uint64_t)blockIdx.x * 32, k0 = (uint64_t)blockIdx.y * 32;
+  for (int i = threadIdx.y; i < 32; i += 8) {
+    const uint64_t k1 = k0 + i, l = l0 + threadIdx.x;
+    uint64_t v = 0;
+    if (k1 < q && l < L) v = k1 == 0 ? X0[l] : gl_add(x0[l], conv[(uint64_t)kpos[k1] * L + l]);
+    tile[i][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += 8) {
+    const uint64_t l = l0 + i, k1 = k0 + threadIdx.x;
+    if (k1 < q && l < L) {
+      const uint64_t j2 = l / C, c = l - j2 * C;
+      Y[(j2 * q + k1) * C + c] = gl_mul(tile[threadIdx.x][i], gl_tw2(tw_lo, tw_hi, j2 * k1));
+    }
+  }
+}
+
 int gl_rader_tables(gl_plan *pl, gl_dev_tables &t) {
   const uint64_t q = pl->q, n = pl->size, r = q - 1;
   std::vector<uint32_t> gp(r), gn(r);
@@ -110,8 +135,11 @@ int gl_rader_tables(gl_plan *pl, gl_dev_tables &t) {
     a = a * kGen % q;
   }
   for (uint64_t p = 0; p < r; p++) gn[p] = gp[(r - p) % r];  // g^-p = g^(q-1-p)
+  std::vector<uint32_t> kp(q, 0);                               // kpos[g^-p] = p
+  for (uint64_t p = 0; p < r; p++) kp[gn[p]] = (uint32_t)p;
   int st = upload(t, gp, &t.rader_gpow);
   if (st == GL_OK) st = upload(t, gn, &t.rader_gneg);
+  if (st == GL_OK) st = upload(t, kp, &t.rader_kpos);
   const uint64_t hi_count = (n + GL_TW_SPLIT - 1) / GL_TW_SPLIT;
   for (int d = 0; d < 2 && st == GL_OK; d++) {
     // omega_n^e (inverse: scaled by 1/q, the part of 1/n the plan of m does not apply)
@@ -174,9 +202,15 @@ int gl_rader_enqueue(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64_t C
     if ((st = gl_cuda_status(cudaGetLastError())) != GL_OK) return st;
     if ((st = gl_enqueue_transform(pl->pq, A, A, L, 1, r * L, true, sub, stream)) != GL_OK) return st;
     uint64_t *target = m > 1 ? Y : out;
-    gl_rader_scatter_kernel<<<grid_for(q * L), 256, 0, stream>>>(A, x0, X0, target, t->rader_gneg,
-                                                                 t->rader_tw_lo[d], t->rader_tw_hi[d],
-                                                                 C, L, (uint32_t)q);
+    if (C < 8) {
+      const dim3 grid((unsigned)((L + 31) / 32), (unsigned)((q + 31) / 32));
+      gl_rader_scatter_tiled_kernel<<<grid, dim3(32, 8), 0, stream>>>(
+          A, x0, X0, target, t->rader_kpos, t->rader_tw_lo[d], t->rader_tw_hi[d], C, L, (uint32_t)q);
+    } else {
+      gl_rader_scatter_kernel<<<grid_for(q * L), 256, 0, stream>>>(A, x0, X0, target, t->rader_gneg,
+                                                                   t->rader_tw_lo[d], t->rader_tw_hi[d],
+                                                                   C, L, (uint32_t)q);
+    }
     if ((st = gl_cuda_status(cudaGetLastError())) != GL_OK) return st;
     if (m > 1 && (st = gl_enqueue_transform(pl->pm, Y, out, q * C, 1, n * C, inv, sub, stream)) != GL_OK)
       return st;
