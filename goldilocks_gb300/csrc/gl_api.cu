@@ -512,7 +512,7 @@ struct gl_prof_rec {
   cudaEvent_t a, b;
 };
 static std::mutex g_prof_mu;
-static bool g_prof_on = false;
+static std::atomic<bool> g_prof_on{false};  // read without the lock on every launch
 static std::vector<gl_prof_rec> g_prof;
 
 static std::string kernel_label(const gl_kernel_entry *k, int role) {
@@ -526,7 +526,7 @@ void gl_launch(const gl_kernel_entry *k, int role, const gl_pass_args &a0, dim3 
   gl_pass_args a = a0;
   if (k->generic) { a.gen_r[0] = k->r1; a.gen_r[1] = k->r2; a.gen_r[2] = k->r3; }
   bool on;
-  { std::lock_guard<std::mutex> lk(g_prof_mu); on = g_prof_on; }
+  on = g_prof_on.load(std::memory_order_relaxed);
   if (!on) { k->launch(a, grid, stream); return; }
   gl_prof_rec r{k, role, elements, nullptr, nullptr};
   cudaEventCreate(&r.a);

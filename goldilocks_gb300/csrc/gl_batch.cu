@@ -38,6 +38,7 @@ struct gl_work {
 };
 
 constexpr int kNT = 1024;
+std::atomic<uint64_t> g_batch_optin{0};
 
 // Shapes the persistent kernel is compiled for: (r1, r2, r3, lanes per work
 // item), forward then inverse; index = 2 * position + inverse.  The lane
@@ -309,7 +310,7 @@ int enqueue_persistent(const gl_poly *polys, uint64_t count, const std::vector<p
     return gl_cuda_status(e);
   uint32_t *ctr = (uint32_t *)(base + o_ctr);
   const size_t smem = max_shape_smem();
-  cudaFuncSetAttribute(gl_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  gl_smem_optin(g_batch_optin, gl_batch_kernel, smem);
   const unsigned grid = (unsigned)std::min<size_t>((size_t)sms, items.size());
   gl_batch_kernel<<<grid, kNT, smem, stream>>>((const gl_work *)(base + o_items), (uint32_t)items.size(),
                                                (const gl_pass_args *)base, ctr, ctr + 2, ctr + 1,
@@ -556,7 +557,7 @@ extern "C" int gl_batch_wait_selftest(uint64_t wait_ns, uint32_t *status) {
   }
   uint32_t *ctr = (uint32_t *)(base + o_ctr);
   const size_t smem = max_shape_smem();
-  cudaFuncSetAttribute(gl_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  gl_smem_optin(g_batch_optin, gl_batch_kernel, smem);
   gl_batch_kernel<<<1, kNT, smem>>>((const gl_work *)(base + o_items), 1u, (const gl_pass_args *)(base + o_args),
                                     ctr, ctr + 2, ctr + 1, wait_ns);
   e = cudaGetLastError();

@@ -4,6 +4,7 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <string>
@@ -60,6 +61,20 @@ const gl_kernel_entry *gl_kernels_wide_inv(size_t *count);
 void gl_launch_generic_fwd(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
 void gl_launch_generic_inv(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
 #include "gl_generic.cuh"
+
+// Opt in to more than 48 KB of dynamic shared memory once per kernel and
+// device (`done` is the calling launcher's own bit set of devices): setting the
+// attribute on every launch costs microseconds of host time per call.
+template <typename K>
+inline void gl_smem_optin(std::atomic<uint64_t> &done, K kern, size_t smem) {
+  if (smem <= 48 * 1024) return;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  const uint64_t bit = 1ull << (dev & 63);
+  if (done.load(std::memory_order_acquire) & bit) return;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess)
+    done.fetch_or(bit, std::memory_order_acq_rel);
+}
 
 // CTAs that cover `lanes` lanes with kernel k.
 inline uint64_t gl_tiles(uint64_t lanes, const gl_kernel_entry *k) { return (lanes + k->lanes - 1) / k->lanes; }

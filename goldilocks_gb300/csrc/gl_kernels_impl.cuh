@@ -7,8 +7,8 @@ template <int MA, int MB, int LANES, bool INV>
 static void gl_launch_pass(const gl_pass_args &args, dim3 grid, cudaStream_t stream) {
   constexpr size_t smem = gl_pass_smem_bytes<MA, MB>(LANES);
   auto kern = gl_pass_kernel<MA, MB, LANES, INV>;
-  // The opt-in is per device context; setting it again is cheap and idempotent.
-  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static std::atomic<uint64_t> optin{0};
+  gl_smem_optin(optin, kern, smem);
   kern<<<grid, LANES * MB, smem, stream>>>(args);
 }
 
@@ -16,7 +16,8 @@ template <int R1, int R2, int R3, int LANES, int NT, bool INV, int MINB = 1>
 static void gl_launch_pass3(const gl_pass_args &args, dim3 grid, cudaStream_t stream) {
   constexpr size_t smem = gl_p3_smem_bytes<R1, R2, R3, LANES>();
   auto kern = gl_pass3_kernel<R1, R2, R3, LANES, NT, INV, MINB>;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static std::atomic<uint64_t> optin{0};
+  gl_smem_optin(optin, kern, smem);
   kern<<<grid, NT, smem, stream>>>(args);
 }
 
