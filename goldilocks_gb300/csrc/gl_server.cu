@@ -100,6 +100,8 @@ int footprint(const gl_request &r, uint64_t *bytes) {
 
 void CUDART_CB on_batch_done(void *arg);
 
+constexpr size_t kDirectMax = 2;  // single-column batches up to this size skip the persistent kernel
+
 struct done_ctx {
   gl_server *srv;
   int slot;
@@ -133,8 +135,19 @@ int launch_batch(gl_server *s, int si, std::vector<std::shared_ptr<job>> &batch)
     if (rc != GL_OK) break;
   }
   *sl.err = 0;
-  if (rc == GL_OK && !polys.empty())
-    rc = gl_batch_enqueue_persistent(polys.data(), polys.size(), st, sl.err);
+  if (rc == GL_OK && !polys.empty()) {
+    if (polys.size() <= kDirectMax) {
+      // A lone request: plain launches on the slot's stream; the persistent
+      // kernel's work-list upload would cost more than it saves.
+      for (const gl_poly &p : polys) {
+        rc = p.dir == GL_INVERSE ? gl_intt(p.data, p.len, GL_MEM_DEVICE, st)
+                                 : gl_ntt(p.data, p.len, GL_MEM_DEVICE, st);
+        if (rc != GL_OK) break;
+      }
+    } else {
+      rc = gl_batch_enqueue_persistent(polys.data(), polys.size(), st, sl.err);
+    }
+  }
   sl.launch_status = rc;
   done_ctx *ctx = new done_ctx{s, si};
   cudaError_t e = cudaLaunchHostFunc(st, on_batch_done, ctx);
