@@ -52,6 +52,22 @@ def env_rank():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def max_over_ranks(dist, x, device):
+    """The largest value of x over all ranks (x itself without a process
+    group): a step counts as long as its slowest replica."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, units_per_rank, seconds):
+    """Units processed by all replicas per second of the slowest one."""
+    return world * units_per_rank / seconds
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -374,11 +390,8 @@ def run_ours(args):
              "total_ms": float(e.total_ms)} for e in ents[:n_ent]]
     launches = sum(p["launches"] for p in prof)
 
-    if dist:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * elements_per_step * args.steps / (total_ms * 1e-3)
+    total_ms = max_over_ranks(dist, total_ms, "cuda")
+    value = whole_job_rate(world, elements_per_step * args.steps, total_ms * 1e-3)
 
     # ---- end to end through the public API with pinned host buffers ----
     hosts = []
@@ -409,19 +422,14 @@ def run_ours(args):
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             fn()
-        s = time.perf_counter() - t0
-        if dist:
-            t = torch.tensor([s], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            s = float(t.item())
-        return s
+        return max_over_ranks(dist, time.perf_counter() - t0, "cuda")
     e2e_s = timed(host_step)
     per_call_s = timed(host_step_per_call)
     step_bytes = 8 * sum(SIZES)  # every buffer in once and out once
-    e2e = {"value": world * elements_per_step * e2e_steps / e2e_s, "unit": UNIT,
+    e2e = {"value": whole_job_rate(world, elements_per_step * e2e_steps, e2e_s), "unit": UNIT,
            "h2d_bytes_per_step": step_bytes, "d2h_bytes_per_step": step_bytes,
            "steps": e2e_steps, "memory": "pinned host", "api": "gl_host_pipeline",
-           "per_call": {"value": world * elements_per_step * e2e_steps / per_call_s,
+           "per_call": {"value": whole_job_rate(world, elements_per_step * e2e_steps, per_call_s),
                         "h2d_bytes_per_step": 2 * step_bytes, "d2h_bytes_per_step": 2 * step_bytes,
                         "api": "gl_plan_execute per transform (GL_MEM_HOST)"}}
 
