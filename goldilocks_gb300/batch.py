@@ -6,7 +6,8 @@
 Each entry is a contiguous CUDA int64/uint64 tensor transformed in place (its
 length must divide p - 1).  Modes: PERSISTENT (one launch, device work queue),
 BUCKETS (per-size launches replayed from a CUDA graph), PER_CALL (one call per
-polynomial), AUTO (the mode `autotune` measured fastest for this batch shape).
+polynomial), AUTO (the mode `autotune` measured fastest for this batch shape,
+else BUCKETS).
 """
 import ctypes
 

@@ -214,7 +214,7 @@ enum { GL_BATCH_AUTO = 0, GL_BATCH_PERSISTENT = 1, GL_BATCH_BUCKETS = 2, GL_BATC
  * GL_BATCH_BUCKETS: launches per (size, direction) bucket, replayed from a
  * CUDA graph cached per batch shape; GL_BATCH_PER_CALL: one gl_ntt/gl_intt per
  * polynomial; GL_BATCH_AUTO: the mode gl_batch_autotune chose for this batch
- * shape, else persistent.  Sizes the persistent and bucket kernels are not
+ * shape, else buckets.  Sizes the persistent and bucket kernels are not
  * built for run per call.  Bounded waits: GL_ERR_TIMEOUT if a dependency did
  * not complete within 2 s. */
 int gl_batch_execute(const gl_poly *polys, uint64_t count, int mode, void *stream);
