@@ -313,6 +313,38 @@ def bench_pow(torch):
             "hashes_per_s": (1 << 33) / scan_s}
 
 
+def bench_small(gl, torch):
+    """The reference's CPU-runnable case: one transform of n = 2^16 and a round
+    trip.  Device-resident time per forward call (200 back to back), the
+    synchronous round trip of a host buffer through the drop-in API, and the
+    oracle's single-thread forward time on the same input."""
+    import numpy as np
+    import oracle
+    n = 1 << 16
+    x = gl.fill_uniform(n, seed=0x5EED0001)
+    d = torch.from_numpy(x.view(np.int64)).cuda()
+    pl = gl.strategy(n)
+    fwd_ms = _time_ms(torch, lambda: pl.ntt(d), 200)
+    h = torch.empty(n, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+    h[:] = x
+    pl.ntt(h)
+    pl.intt(h)
+    t = time.perf_counter()
+    for _ in range(50):
+        pl.ntt(h)
+        pl.intt(h)
+    rt_us = (time.perf_counter() - t) / 50 * 1e6
+    assert np.array_equal(h, x)
+    oracle.build()
+    oracle.ntt(x)
+    t = time.perf_counter()
+    for _ in range(5):
+        oracle.ntt(x)
+    cpu_us = (time.perf_counter() - t) / 5 * 1e6
+    return {"n": n, "fwd_us_device": fwd_ms * 1e3, "roundtrip_us_host_memory": rt_us,
+            "cpu_oracle_fwd_us_1_thread": cpu_us}
+
+
 def cpu_oracle_k12_rate(seconds=2.0):
     """Single-thread rate of the K12 oracle (C restatement of
     pcs/src/k12/generic.rs) on 160-byte blocks."""
@@ -476,7 +508,8 @@ def run_ours(args):
             line["serving"] = bench_serving(gl, torch)
         except Exception as e:
             line["serving"] = {"error": str(e)}
-        for key, fn in (("commit", lambda: bench_commit(gl, torch)),
+        for key, fn in (("small_2p16", lambda: bench_small(gl, torch)),
+                        ("commit", lambda: bench_commit(gl, torch)),
                         ("convolve", lambda: bench_convolve(gl, torch)),
                         ("pow", lambda: bench_pow(torch))):
             try:
@@ -507,7 +540,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the batched, serving, commit, convolve and proof-of-work figures")
+                    help="skip the small-transform, batched, serving, commit, convolve and "
+                         "proof-of-work figures")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
