@@ -11,11 +11,14 @@
  * the path is F_p-linear.  Outputs are fully reduced (< p).  Inputs >= p are
  * accepted and treated as their residue mod p.
  *
- * Memory: `mem` says where `data` lives.  GL_MEM_HOST: the call copies to the
- * GPU, runs, copies back and returns when the result is in `data`
- * (synchronous, like the reference).  GL_MEM_DEVICE: `data` is device memory;
- * the work is queued on `stream` (a cudaStream_t, NULL = legacy default
- * stream) and the call returns without waiting.
+ * Memory: `mem` says where `data` lives.  GL_MEM_HOST: the call returns when
+ * the result is in `data` (synchronous, like the reference).  Pageable memory
+ * is copied to the GPU and back; page-locked memory (cudaHostAlloc,
+ * cudaMallocHost, cudaHostRegister) is read by the first pass and written by
+ * the last one in place, over the host link.  Either way `data` must be one
+ * allocation of at least `len` words.  GL_MEM_DEVICE: `data` is device
+ * memory; the work is queued on `stream` (a cudaStream_t, NULL = legacy
+ * default stream) and the call returns without waiting.
  *
  * Errors: every call returns a gl_status.  The reference panics on an
  * unsupported size ("{size} is not a supported NTT size (does not divide
