@@ -659,6 +659,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
     gl_pass_args a = base_args();
     a.tw_m = inv ? t->blk_scaled_inv : t->blk[0][0];
     a.tw_r2 = t->blk[0][d];
+    a.flags |= GL_PF_CANON_IN;
     if (inv) a.flags |= GL_PF_SCALE_ALL;
     if (coset) {
       a.flags |= GL_PF_IN_TWIDDLE;
@@ -714,7 +715,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       a.in = in; a.out = s1;
       a.in_ls = a.out_ls = 1; a.in_is = a.out_is = (int64_t)(n23 * C);
       a.lanes = (uint32_t)(n23 * C);
-      a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
+      a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST | GL_PF_CANON_IN;
       a.tw_m = a.tw_r2 = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
       a.tw_lane_div = (uint32_t)C;
       if (coset) {
@@ -779,7 +780,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
     a.in_ls = a.out_ls = 1; a.in_is = a.out_is = (int64_t)(n2 * C);
     a.in_bs = (int64_t)bs; a.out_bs = (int64_t)(n * C);
     a.lanes = (uint32_t)(n2 * C);
-    a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
+    a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST | GL_PF_CANON_IN;
     a.tw_m = a.tw_r2 = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
     a.tw_lane_div = (uint32_t)C;
     if (t->tw_full[d]) {
@@ -850,7 +851,7 @@ int gl_enqueue_pass_range(gl_plan *pl, int stage, const uint64_t *src, uint64_t 
     const gl_kernel_entry *kc = pl->k[0][d];
     a.in = src + lo; a.out = dst + lo;
     a.in_ls = a.out_ls = 1; a.in_is = a.out_is = (int64_t)n2;
-    a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
+    a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST | GL_PF_CANON_IN;
     a.tw_m = a.tw_r2 = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
     a.tw_col0 = lo;
     GL_DBG_EXTENTS(a, n1 * n2 - lo, n1 * n2 - lo);

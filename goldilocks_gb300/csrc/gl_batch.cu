@@ -180,6 +180,7 @@ void pass_args(const poly_plan &pp, uint64_t *data, uint64_t *scratch, gl_pass_a
     a.tw_lane_div = 1;
     a.tw_m = pp.inv ? t->blk_scaled_inv : t->blk[0][0];
     a.tw_r2 = t->blk[0][d];
+    a.flags |= GL_PF_CANON_IN;
     if (pp.inv) a.flags |= GL_PF_SCALE_ALL;
     *full = a;
     return;
@@ -191,7 +192,7 @@ void pass_args(const poly_plan &pp, uint64_t *data, uint64_t *scratch, gl_pass_a
   a.lanes = (uint32_t)n2;
   a.in_limit = 0xffffffffu;
   a.tw_lane_div = 1;
-  a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
+  a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST | GL_PF_CANON_IN;
   a.tw_m = a.tw_r2 = t->blk[0][d];
   a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
   if (t->tw_full[d]) { a.flags |= GL_PF_TW_TABLE; a.tw_full = t->tw_full[d]; a.tw_ld = (int64_t)n2; }

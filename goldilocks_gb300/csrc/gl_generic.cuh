@@ -64,6 +64,10 @@ __device__ __forceinline__ void gl_gen_round1(const gl_pass_args &a, const gl_ge
       const uint64_t *p = src + (int64_t)(q.S1 * t) * a.in_is;
       x[t] = (live && j < a.in_limit) ? gl_ld_in(a, p, (a.flags & GL_PF_LOAD_CG) != 0) : 0;
     }
+    if ((a.flags & (GL_PF_CANON_IN | GL_PF_IN_TWIDDLE)) == GL_PF_CANON_IN) {
+#pragma unroll
+      for (int t = 0; t < R; t++) x[t] = gl_canon(x[t]);
+    }
     if ((a.flags & GL_PF_IN_TWIDDLE) && live) {
       const uint64_t col = (uint64_t)lane / a.tw_lane_div;
 #pragma unroll

@@ -112,7 +112,7 @@ extern "C" int gl_ntt_noalloc(uint64_t *data, uint64_t len, int dir, void *strea
   a.in = data; a.out = p.scratch;
   a.in_ls = a.out_ls = 1; a.in_is = a.out_is = (int64_t)n2;
   a.lanes = (uint32_t)n2;
-  a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
+  a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST | GL_PF_CANON_IN;
   a.in_limit = 0xffffffffu;
   a.tw_lane_div = 1;
   a.tw_m = a.tw_r2 = tab + GL_NOALLOC_T1;

@@ -31,6 +31,7 @@ enum : uint32_t {
   GL_PF_PTR_TABLE = 128u,      // batch item by = in_ptrs[by] / out_ptrs[by] (no *_bs)
   GL_PF_OUT_MUL = 256u,        // final store: outputs *= mul[...] (pointwise spectrum product)
   GL_PF_OUT_MUL_MONT = 512u,   // ... and * 2^-64 (product of two Montgomery words)
+  GL_PF_CANON_IN = 1024u,      // inputs may be >= p: reduce them on load (first pass of a call)
 };
 
 struct gl_pass_args {
@@ -169,6 +170,10 @@ gl_pass_kernel(const gl_pass_args a) {
     for (int jA = 0; jA < MA; jA++) {
       const uint32_t j = (uint32_t)(MB * jA + jB);
       x[jA] = (live && j < a.in_limit) ? src[(int64_t)(MB * jA) * a.in_is] : 0;
+    }
+    if ((a.flags & (GL_PF_CANON_IN | GL_PF_IN_TWIDDLE)) == GL_PF_CANON_IN) {
+#pragma unroll
+      for (int jA = 0; jA < MA; jA++) x[jA] = gl_canon(x[jA]);
     }
     if (a.flags & GL_PF_IN_TWIDDLE) {
       const uint64_t col = (uint64_t)(lane0 + c) / a.tw_lane_div;

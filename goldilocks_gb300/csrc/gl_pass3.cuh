@@ -82,6 +82,12 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
           x[t] = (live && j < a.in_limit) ? gl_ld_in(a, src + (int64_t)(S1 * t) * a.in_is, false) : 0;
         }
       }
+      // Caller data may hold words >= p: the codelets' additions need canonical
+      // operands (the coset factor's Montgomery product reduces them anyway).
+      if ((a.flags & (GL_PF_CANON_IN | GL_PF_IN_TWIDDLE)) == GL_PF_CANON_IN) {
+#pragma unroll
+        for (int t = 0; t < R1; t++) x[t] = gl_canon(x[t]);
+      }
       if (a.flags & GL_PF_IN_TWIDDLE) {
         const uint64_t col = (uint64_t)lane / a.tw_lane_div;
 #pragma unroll

@@ -14,6 +14,7 @@ from conftest import P, ROOT, rand_field
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 F_PASS_TW, F_SCALE, F_LOAD_LF, F_STORE_LF, F_IN_TW = 1, 2, 4, 8, 16
+F_CANON_IN = 1024
 NOLIM = 0xFFFFFFFF
 
 
@@ -174,3 +175,20 @@ def test_debug_checks_flag_and_skip_out_of_range(emu_checked):
     call(emu_checked, (8, 8, 1), False, x, out, 1, cols, 1, cols, cols, F_LOAD_LF | F_STORE_LF, tw, tw)
     assert emu_checked.emu_check_flags() == 1
     emu_checked.emu_set_checks(0, 0)
+
+
+@pytest.mark.parametrize("shape", [(16, 16, 1), ("gen", 17, 15, 1)])
+def test_inputs_above_p_are_reduced(emu, oracle, shape):
+    """Words in [p, 2^64) are their residue: the first pass of a call reduces
+    them on load (GL_PF_CANON_IN) before the codelets' additions."""
+    r = shape[1:] if shape[0] == "gen" else shape
+    m, cols = r[0] * r[1] * r[2], 3
+    x = rand_field(m * cols, seed=21)
+    x[::2] = np.random.default_rng(22).integers(0, 2**32 - 1, size=x[::2].size, dtype=np.uint64)
+    xn = x.copy()
+    xn[::2] += np.uint64(P)                      # the same residues, non-canonical words
+    out = np.zeros_like(x)
+    tw = table(root(m), m)
+    call(emu, shape, False, xn, out, 1, cols, 1, cols, cols, F_LOAD_LF | F_STORE_LF | F_CANON_IN, tw, tw)
+    want = np.stack([oracle.ntt(x.reshape(m, cols)[:, c].copy()) for c in range(cols)], axis=1)
+    assert np.array_equal(out.reshape(m, cols), want)

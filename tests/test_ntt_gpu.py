@@ -133,6 +133,22 @@ def test_edge_values(gl, oracle, cuda):
     assert np.array_equal(from_dev(d), oracle.ntt(x))
 
 
+@pytest.mark.parametrize("n", [4096, 1 << 16, 1 << 24, 257 * 16, 1 << 25, 3 * 5 * 17])
+def test_words_above_p_are_their_residue(gl, oracle, cuda, n):
+    """The header accepts words >= p and treats them as their residue mod p."""
+    x = gl.fill_uniform(n, seed=n)
+    small = np.random.default_rng(n).integers(0, 2**32 - 1, size=(n + 1) // 2, dtype=np.uint64)
+    x[::2] = small
+    xn = x.copy()
+    xn[::2] += np.uint64(P)
+    d = to_dev(cuda, xn)
+    gl.ntt(d)
+    assert np.array_equal(from_dev(d), oracle.ntt(x))
+    d = to_dev(cuda, xn)
+    gl.intt(d)
+    assert np.array_equal(from_dev(d), oracle.intt(x))
+
+
 def test_unsupported_size_raises(gl, cuda):
     d = cuda.zeros(7, dtype=cuda.int64, device="cuda")
     with pytest.raises(ValueError, match="is not a supported NTT size"):
