@@ -106,3 +106,19 @@ def test_injected_allocation_failures_propagate(gl, cuda):
     gl.ntt(d)                                             # and the library keeps working
     gl.intt(d)
     assert np.array_equal(d.cpu().numpy().view(np.uint64), x)
+
+
+@pytest.mark.parametrize("mode_name", ["persistent", "buckets", "auto"])
+def test_batch_with_three_pass_and_rader_lengths(gl, oracle, cuda, mode_name):
+    """Lengths the persistent and bucket kernels have no shape for (three
+    passes, Rader steps, run-time radices) run as plain calls inside the
+    batch, in order with the rest."""
+    from goldilocks_gb300 import batch as B
+    mode = {"persistent": B.PERSISTENT, "buckets": B.BUCKETS, "auto": B.AUTO}[mode_name]
+    sizes = [1 << 25, 4096, 257 * 16, 1 << 16, 3 << 10, 65537, 1 << 18]
+    xs = [gl.fill_uniform(n, seed=i) for i, n in enumerate(sizes)]
+    ds = [to_dev(cuda, x) for x in xs]
+    dirs = [i % 2 for i in range(len(sizes))]
+    B.run(list(zip(ds, dirs)), mode=mode)
+    for x, d, inv in zip(xs, ds, dirs):
+        assert np.array_equal(from_dev(d), (oracle.intt if inv else oracle.ntt)(x)), x.size

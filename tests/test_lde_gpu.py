@@ -25,7 +25,8 @@ def lde_call(gl, cuda, d, out, n, cols, blowup, shift):
 
 
 @pytest.mark.parametrize("rows,cols", [(8, 3), (64, 5), (1024, 4), (4096, 7), (1 << 13, 4),
-                                       (1 << 14, 6), (1 << 16, 2), (1 << 12, 64)])
+                                       (1 << 14, 6), (1 << 16, 2), (1 << 12, 64), (1 << 16, 1),
+                                       (2, 5)])
 def test_columns_match_oracle(gl, oracle, cuda, rows, cols):
     x = rand_field(rows * cols, seed=rows + cols)
     d = to_dev(cuda, x)
@@ -39,7 +40,8 @@ def test_columns_match_oracle(gl, oracle, cuda, rows, cols):
 
 
 @pytest.mark.parametrize("n,cols,blowup", [(16, 3, 4), (64, 4, 2), (1024, 8, 4), (4096, 5, 4),
-                                           (1 << 13, 4, 2), (1 << 14, 4, 4), (1 << 12, 16, 8)])
+                                           (1 << 13, 4, 2), (1 << 14, 4, 4), (1 << 12, 16, 8),
+                                           (1024, 3, 1), (1 << 16, 2, 1), (2, 3, 4), (1, 4, 8)])
 def test_lde_matches_oracle(gl, oracle, cuda, n, cols, blowup):
     x = rand_field(n * cols, seed=n * cols + blowup)
     d = to_dev(cuda, x)
