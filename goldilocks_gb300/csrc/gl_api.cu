@@ -941,6 +941,9 @@ void *gl_host_device_view(const void *p, uint64_t bytes) {
   return a0.devicePointer;
 }
 
+// Host-memory calls from this many words on move in column blocks.
+static const uint64_t kHostBlocksMinWords = 1ull << 21;
+
 static int execute(gl_plan *pl, uint64_t *data, uint64_t len, int dir, int mem, void *ws,
                    uint64_t ws_bytes, cudaStream_t stream) {
   if (!pl || (!data && len)) return GL_ERR_INVALID;
@@ -967,9 +970,21 @@ static int execute(gl_plan *pl, uint64_t *data, uint64_t len, int dir, int mem, 
     if (own) cudaFreeAsync(scratch, stream);
     return st;
   }
+  // A large two-pass transform of page-locked memory: copied in column blocks
+  // overlapped with its column pass and out in blocks overlapped with its row
+  // pass (the pipeline of gl_host_pipeline with one job), after the caller's
+  // stream has drained so that stream order holds.
+  void *hview = gl_host_device_view(data, len * sizeof(uint64_t));
+  if (hview && pl->kind == 2 && count == 1 && len >= kHostBlocksMinWords) {
+    cudaError_t e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return gl_cuda_status(e);
+    gl_host_job job{};
+    job.data = data; job.len = len; job.count = 1; job.nops = 1; job.dirs[0] = dir;
+    return gl_host_pipeline(&job, 1, 1);
+  }
   // Host memory the GPU addresses directly: the first pass reads it and the
   // last pass writes it; only the scratch lives in device memory.
-  if (uint64_t *hv = (uint64_t *)gl_host_device_view(data, len * sizeof(uint64_t))) {
+  if (uint64_t *hv = (uint64_t *)hview) {
     uint64_t *scratch = nullptr;
     if (need) {
       cudaError_t e = gl_malloc_async((void **)&scratch, need, stream);
