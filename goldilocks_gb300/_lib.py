@@ -51,6 +51,10 @@ SIGNATURES = [
     ("gl_pow_solve", _int, [_vp, _u64, _u64, _u64, _u64p, _vp]),
     ("gl_batch_execute", _int, [_vp, _u64, _int, _vp]),
     ("gl_batch_autotune", _int, [_vp, _u64, _int, _vp, _vp]),
+    ("gl_plan_autotune", _int, [_u64, _int, _vp, _vp]),
+    ("gl_tune_save", _int, [ctypes.c_char_p]),
+    ("gl_tune_load", _int, [ctypes.c_char_p]),
+    ("gl_tune_clear", None, []),
     ("gl_server_create", _int, [_u64, _int, _int, ctypes.POINTER(_vp)]),
     ("gl_server_request_bytes", _int, [_vp, ctypes.POINTER(_u64)]),
     ("gl_server_submit", _int, [_vp, _vp, ctypes.POINTER(_u64)]),
@@ -112,6 +116,8 @@ GL_ERR_CUDA = 6
 GL_ERR_BUSY = 7
 GL_ERR_CANCELLED = 8
 GL_ERR_NOT_FOUND = 9
+GL_ERR_IO = 10
+GL_ERR_VERIFY = 11
 GL_FORWARD, GL_INVERSE = 0, 1
 GL_MEM_HOST, GL_MEM_DEVICE = 0, 1
 

@@ -45,6 +45,8 @@ extern "C" const char *gl_status_string(int status) {
     case GL_ERR_BUSY: return "queue full";
     case GL_ERR_CANCELLED: return "cancelled";
     case GL_ERR_NOT_FOUND: return "unknown request";
+    case GL_ERR_IO: return "file could not be read or written";
+    case GL_ERR_VERIFY: return "schedules disagreed";
     default: return "unknown status";
   }
 }
@@ -235,50 +237,39 @@ static uint64_t h_root(uint64_t order, bool inv) {
 // Pass sizes the COL/ROW kernels are built for.
 static bool pass_size_ok(uint64_t m) { return gl_find_kernel(m, false, false) != nullptr; }
 
-static void choose_schedule(gl_plan *pl) {
-  uint64_t n = pl->size;
-  if (n <= 1) { pl->kind = 0; return; }
-  if (gl_find_kernel(n, true, false)) {
-    pl->kind = 1;
-    for (int d = 0; d < 2; d++) pl->k[0][d] = gl_find_kernel(n, true, d == 1);
-    return;
-  }
+static bool split_ok(uint64_t m) { return m >= GL_PASS_LANES && m % GL_PASS_LANES == 0 && pass_size_ok(m); }
+
+gl_choice gl_choice_default(uint64_t n) {
+  gl_choice c;
+  if (n <= 1) { c.kind = 0; return c; }
+  if (gl_find_kernel(n, true, false)) { c.kind = 1; return c; }
   // Four-step: prefer n1 <= n2 nearest sqrt(n), both with pass kernels.
   uint64_t best1 = 0;
   for (uint64_t n1 : divisor_list()) {
     if (n1 > n) break;
     if (n % n1) continue;
     uint64_t n2 = n / n1;
-    if (!pass_size_ok(n1) || !pass_size_ok(n2)) continue;
-    if (n1 % GL_PASS_LANES || n2 % GL_PASS_LANES) continue;
+    if (!split_ok(n1) || !split_ok(n2)) continue;
     if (best1 == 0 || (std::max(n1, n2) < std::max(best1, n / best1)) ||
         (std::max(n1, n2) == std::max(best1, n / best1) && n1 > best1))
       best1 = n1;
   }
   if (best1) {
-    pl->kind = 2;
-    pl->n1 = best1;
-    pl->n2 = n / best1;
-    for (int d = 0; d < 2; d++) {
-      pl->k[0][d] = gl_find_kernel(pl->n1, false, d == 1);
-      pl->k[1][d] = gl_find_kernel(pl->n2, false, d == 1);
-      pl->k4[0][d] = gl_find_kernel_cols(pl->n1, d == 1);
-      pl->k4[1][d] = gl_find_kernel_cols(pl->n2, d == 1);
-    }
-    return;
+    c.kind = 2;
+    c.n1 = best1;
+    c.n2 = n / best1;
+    return c;
   }
   // Three passes for n beyond 4096^2: n = n1*n2*n3, all with pass kernels,
   // the largest factor as small as possible.
   uint64_t b1 = 0, b2 = 0;
   for (uint64_t n1 : divisor_list()) {
     if (n1 > 4096) break;
-    if (n % n1 || !pass_size_ok(n1) || n1 % GL_PASS_LANES) continue;
+    if (n % n1 || !split_ok(n1)) continue;
     const uint64_t r = n / n1;
     for (uint64_t n2 : divisor_list()) {
       if (n2 > 4096) break;
-      if (r % n2 || !pass_size_ok(n2) || !pass_size_ok(r / n2) || n2 % GL_PASS_LANES ||
-          (r / n2) % GL_PASS_LANES)
-        continue;
+      if (r % n2 || !split_ok(n2) || !split_ok(r / n2)) continue;
       const uint64_t n3 = r / n2;
       const uint64_t worst = std::max(n1, std::max(n2, n3));
       if (b1 == 0 || worst < std::max(b1, std::max(b2, n / (b1 * b2))))
@@ -286,20 +277,126 @@ static void choose_schedule(gl_plan *pl) {
     }
   }
   if (b1) {
-    pl->kind = 3;
-    pl->n1 = b1;
-    pl->n2 = b2;
-    pl->n3 = n / (b1 * b2);
-    for (int d = 0; d < 2; d++) {
-      pl->k[0][d] = gl_find_kernel(pl->n1, false, d == 1);
-      pl->k[1][d] = gl_find_kernel(pl->n2, false, d == 1);
-      pl->k[2][d] = gl_find_kernel(pl->n3, false, d == 1);
-      for (int s = 0; s < 3; s++)
-        pl->k4[s][d] = gl_find_kernel_cols(s == 0 ? pl->n1 : s == 1 ? pl->n2 : pl->n3, d == 1);
-    }
-    return;
+    c.kind = 3;
+    c.n1 = b1;
+    c.n2 = b2;
+    c.n3 = n / (b1 * b2);
   }
-  pl->kind = -1;  // divisor without a GPU schedule
+  return c;  // kind -1: a divisor without a GPU schedule
+}
+
+static bool same_schedule(const gl_choice &a, const gl_choice &b) {
+  return a.kind == b.kind && a.n1 == b.n1 && a.n2 == b.n2 && a.n3 == b.n3 && a.lanes4 == b.lanes4;
+}
+
+std::vector<gl_choice> gl_choice_candidates(uint64_t n) {
+  std::vector<gl_choice> out;
+  const gl_choice d = gl_choice_default(n);
+  if (d.kind < 0) return out;
+  out.push_back(d);
+  if (d.kind <= 1) return out;  // one pass or none: nothing to choose
+  auto two_lane = [](uint64_t m) { return gl_find_kernel(m, false, false) != gl_find_kernel4(m, false); };
+  auto add = [&](gl_choice c) {
+    for (int l = 0; l < 2; l++) {
+      c.lanes4 = l;
+      if (l && !two_lane(c.n1) && !two_lane(c.n2) && !(c.kind == 3 && two_lane(c.n3))) break;
+      bool dup = false;
+      for (const gl_choice &o : out) dup = dup || same_schedule(o, c);
+      if (!dup) out.push_back(c);
+    }
+  };
+  add(d);  // its lane variant
+  for (uint64_t n1 : divisor_list()) {
+    if (n1 > 4096) break;
+    if (n % n1 || n / n1 > 4096 || !split_ok(n1) || !split_ok(n / n1)) continue;
+    gl_choice c;
+    c.kind = 2; c.n1 = n1; c.n2 = n / n1;
+    add(c);
+  }
+  // Three passes: the few splits with the smallest largest factor (a third
+  // HBM pass costs 1.5x the traffic of two).
+  std::vector<gl_choice> tri;
+  for (uint64_t n1 : divisor_list()) {
+    if (n1 > 4096) break;
+    if (n % n1 || !split_ok(n1)) continue;
+    for (uint64_t n2 : divisor_list()) {
+      if (n2 > 4096) break;
+      const uint64_t r = n / n1;
+      if (r % n2 || r / n2 > 4096 || !split_ok(n2) || !split_ok(r / n2)) continue;
+      gl_choice c;
+      c.kind = 3; c.n1 = n1; c.n2 = n2; c.n3 = r / n2;
+      tri.push_back(c);
+    }
+  }
+  auto worst = [](const gl_choice &c) { return std::max(c.n1, std::max(c.n2, c.n3)); };
+  std::stable_sort(tri.begin(), tri.end(),
+                   [&](const gl_choice &a, const gl_choice &b) { return worst(a) < worst(b); });
+  if (tri.size() > 6) tri.resize(6);
+  for (const gl_choice &c : tri) add(c);
+  return out;
+}
+
+bool gl_choice_apply(gl_plan *pl, const gl_choice &c) {
+  const uint64_t n = pl->size;
+  switch (c.kind) {
+    case 0:
+      if (n > 1) return false;
+      break;
+    case 1:
+      if (!gl_find_kernel(n, true, false)) return false;
+      break;
+    case 2:
+      if (!split_ok(c.n1) || !split_ok(c.n2) || c.n1 * c.n2 != n || c.n3) return false;
+      break;
+    case 3:
+      if (!split_ok(c.n1) || !split_ok(c.n2) || !split_ok(c.n3) || c.n1 * c.n2 * c.n3 != n) return false;
+      break;
+    default:
+      return false;
+  }
+  pl->kind = c.kind;
+  pl->n1 = c.n1;
+  pl->n2 = c.n2;
+  pl->n3 = c.n3;
+  const uint64_t f[3] = {c.n1, c.n2, c.n3};
+  for (int d = 0; d < 2; d++) {
+    if (c.kind == 1) pl->k[0][d] = gl_find_kernel(n, true, d == 1);
+    for (int s = 0; c.kind >= 2 && s < c.kind; s++) {
+      pl->k[s][d] = c.lanes4 ? gl_find_kernel4(f[s], d == 1) : gl_find_kernel(f[s], false, d == 1);
+      pl->k4[s][d] = gl_find_kernel_cols(f[s], d == 1);
+    }
+  }
+  return true;
+}
+
+static std::mutex g_tuned_mu;
+static std::map<uint64_t, gl_choice> g_tuned_plans;
+
+void gl_tuned_set(uint64_t n, const gl_choice &c) {
+  std::lock_guard<std::mutex> lk(g_tuned_mu);
+  g_tuned_plans[n] = c;
+}
+
+void gl_tuned_clear() {
+  std::lock_guard<std::mutex> lk(g_tuned_mu);
+  g_tuned_plans.clear();
+}
+
+std::vector<std::pair<uint64_t, gl_choice>> gl_tuned_list() {
+  std::lock_guard<std::mutex> lk(g_tuned_mu);
+  return std::vector<std::pair<uint64_t, gl_choice>>(g_tuned_plans.begin(), g_tuned_plans.end());
+}
+
+// The tuned schedule of the size if one was measured or loaded, else the
+// default.
+static void choose_schedule(gl_plan *pl) {
+  gl_choice c = gl_choice_default(pl->size);
+  {
+    std::lock_guard<std::mutex> lk(g_tuned_mu);
+    auto it = g_tuned_plans.find(pl->size);
+    if (it != g_tuned_plans.end()) c = it->second;
+  }
+  if (!gl_choice_apply(pl, c)) pl->kind = -1;  // -1: a divisor without a GPU schedule
 }
 
 static int upload(gl_dev_tables &t, const std::vector<uint64_t> &h, uint64_t **dst) {
@@ -467,11 +564,53 @@ uint64_t gl_plan_scratch_words(const gl_plan *pl, uint64_t C, uint64_t B) {
 // but keeps them alive so that handles held by callers stay valid.
 extern "C" void gl_plan_release(gl_plan *) {}
 
+static std::vector<gl_plan *> g_retired;  // guarded by g_cache_mu
+
 extern "C" void gl_clear_cache(void) {
-  static std::vector<gl_plan *> retired;
   std::lock_guard<std::mutex> lk(g_cache_mu);
-  for (auto &kv : g_cache) retired.push_back(kv.second);
+  for (auto &kv : g_cache) g_retired.push_back(kv.second);
   g_cache.clear();
+}
+
+gl_plan *gl_plan_from_choice(uint64_t size, const gl_choice &c) {
+  if (!gl_is_divisor(size) || size % 65537 == 0 || size % 257 == 0) return nullptr;
+  gl_plan *pl = new gl_plan();
+  pl->size = size;
+  pl->tree = reference_tree(size);
+  if (!gl_choice_apply(pl, c)) {
+    delete pl;
+    return nullptr;
+  }
+  return pl;
+}
+
+void gl_plan_free(gl_plan *pl) {
+  if (!pl) return;
+  for (auto &kv : pl->dev)
+    for (void *p : kv.second.owned) cudaFree(p);
+  delete pl;
+}
+
+static void forget_locked(uint64_t n) {
+  for (auto it = g_cache.begin(); it != g_cache.end();) {
+    if (it->first == n || it->second->kind == 4) {
+      g_retired.push_back(it->second);
+      it = g_cache.erase(it);
+    } else {
+      ++it;
+    }
+  }
+}
+
+void gl_plan_forget(uint64_t n) {
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  forget_locked(n);
+}
+
+void gl_plan_install(gl_plan *pl) {
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  forget_locked(pl->size);
+  g_cache[pl->size] = pl;
 }
 
 extern "C" uint64_t gl_plan_len(const gl_plan *plan) { return plan ? plan->size : 0; }
@@ -479,7 +618,11 @@ extern "C" uint64_t gl_plan_len(const gl_plan *plan) { return plan ? plan->size 
 extern "C" int gl_plan_describe(const gl_plan *plan, char *buf, size_t cap) {
   if (!plan || !buf) return GL_ERR_INVALID;
   std::string s = plan->tree + " | gpu: ";
-  auto kname = [](const gl_kernel_entry *k) { return kernel_shape(k); };
+  auto kname = [](const gl_kernel_entry *k) {
+    std::string t = kernel_shape(k);
+    t.insert(t.size() - 1, ", " + std::to_string(k->lanes) + " lanes");
+    return t;
+  };
   if (plan->kind == 0) s += "no-op";
   else if (plan->kind == 1) s += "full " + kname(plan->k[0][0]);
   else if (plan->kind == 2) s += "col " + kname(plan->k[0][0]) + " + row " + kname(plan->k[1][0]);

@@ -536,6 +536,23 @@ extern "C" int gl_batch_autotune(const gl_poly *polys, uint64_t count, int reps,
   return GL_OK;
 }
 
+std::vector<std::pair<gl_batch_shape, int>> gl_batch_tuned_list() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  return std::vector<std::pair<gl_batch_shape, int>>(g_tuned.begin(), g_tuned.end());
+}
+
+void gl_batch_tuned_clear() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tuned.clear();
+}
+
+void gl_batch_tuned_set(const gl_batch_shape &shape, int mode) {
+  gl_batch_shape s = shape;
+  std::sort(s.begin(), s.end());
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tuned[s] = mode;
+}
+
 // Diagnostic: one row-pass work item whose column pass is never queued, so
 // its bounded wait must run out.  The kernel records GL_ERR_TIMEOUT and every
 // CTA returns; the item itself is never executed.

@@ -195,3 +195,41 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
 // word (0 = success) is copied to *err_out afterwards.  (gl_batch.cu)
 int gl_batch_enqueue_persistent(const gl_poly *polys, uint64_t count, cudaStream_t stream,
                                 uint32_t *err_out);
+
+// ------------------------------------------------------------ schedules
+// A transform schedule: kind 1 (FULL), 2 (COL n1 + ROW n2) or 3 (COL n1,
+// COL n2, ROW n3); lanes4 = 1 runs the passes of contiguous transforms
+// (C = 1) on the four-lane kernels instead of the two-lane ones.  (gl_api.cu)
+struct gl_choice {
+  int kind = -1;
+  uint64_t n1 = 0, n2 = 0, n3 = 0;
+  int lanes4 = 0;
+  double ms = 0;  // measured time of one forward transform (0: not measured)
+};
+gl_choice gl_choice_default(uint64_t n);
+// The default first, then the other valid splits (and lane variants).
+std::vector<gl_choice> gl_choice_candidates(uint64_t n);
+bool gl_choice_apply(gl_plan *pl, const gl_choice &c);
+// A plan of `size` scheduled by `c`, outside the cache; null if c is not a
+// valid schedule of size.  gl_plan_free releases its device tables (the
+// device must be done with them) and the plan.
+gl_plan *gl_plan_from_choice(uint64_t size, const gl_choice &c);
+void gl_plan_free(gl_plan *pl);
+// Tuned schedules, consulted whenever a plan is built.
+void gl_tuned_set(uint64_t n, const gl_choice &c);
+std::vector<std::pair<uint64_t, gl_choice>> gl_tuned_list();
+void gl_tuned_clear();
+// Make `pl` the cached plan of its size.  The plan it replaces is retired
+// (kept alive for handles callers hold), and cached Rader plans are dropped
+// so that they are rebuilt over the current sub-plans.
+void gl_plan_install(gl_plan *pl);
+// Drop every cached plan of size n (and the Rader plans); the next
+// gl_plan_create builds it again.
+void gl_plan_forget(uint64_t n);
+
+// Tuned batch modes per batch shape (sorted (length, direction) pairs).
+// (gl_batch.cu)
+typedef std::vector<std::pair<uint64_t, int>> gl_batch_shape;
+std::vector<std::pair<gl_batch_shape, int>> gl_batch_tuned_list();
+void gl_batch_tuned_set(const gl_batch_shape &shape, int mode);
+void gl_batch_tuned_clear();

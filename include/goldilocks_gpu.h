@@ -46,7 +46,9 @@ typedef enum {
   GL_ERR_CUDA = 6,             /* a CUDA runtime call failed */
   GL_ERR_BUSY = 7,             /* queue full; retry later */
   GL_ERR_CANCELLED = 8,        /* request cancelled before it ran */
-  GL_ERR_NOT_FOUND = 9         /* unknown request id */
+  GL_ERR_NOT_FOUND = 9,        /* unknown request id */
+  GL_ERR_IO = 10,              /* a file could not be read or written */
+  GL_ERR_VERIFY = 11           /* two schedules of one size disagreed (autotuning) */
 } gl_status;
 
 enum { GL_FORWARD = 0, GL_INVERSE = 1 };
@@ -225,6 +227,32 @@ int gl_batch_execute(const gl_poly *polys, uint64_t count, int mode, void *strea
  * ms_out[0..2] when non-null) and remember the fastest for this batch shape.
  * The polynomials are transformed (1 + reps) times per mode. */
 int gl_batch_autotune(const gl_poly *polys, uint64_t count, int reps, void *stream, double *ms_out);
+
+/* ---- schedule tuning (no counterpart in the reference, whose strategy()
+ * is a fixed rule: ntt/src/ntt/mod.rs:48-78) ---- */
+
+/* Time every candidate schedule of `size` (two- and three-pass splits, two-
+ * and four-lane pass kernels; `reps` forward transforms each on seeded device
+ * buffers, after one untimed run), check that every candidate's output equals
+ * the default schedule's word for word (GL_ERR_VERIFY if not), and make the
+ * fastest the plan of `size` from now on (a candidate must beat the default
+ * by 2%).  Plans handed out earlier stay valid and keep their schedule.
+ * Rader sizes (factor 257 or 65537) tune their two sub-plans.  ms_out[0] =
+ * the default's mean ms per transform, ms_out[1] = the chosen one's, when
+ * non-null.  Needs about 32 bytes of device memory per element. */
+int gl_plan_autotune(uint64_t size, int reps, void *stream, double *ms_out);
+/* Write the tuned schedules and batch modes (gl_plan_autotune,
+ * gl_batch_autotune, gl_tune_load) to `path` as JSON; GL_ERR_IO if it cannot
+ * be written. */
+int gl_tune_save(const char *path);
+/* Read a file gl_tune_save wrote (or one in its format): GL_ERR_IO if it
+ * cannot be read, GL_ERR_INVALID (nothing applied) if it is not valid JSON in
+ * that format or names a schedule that is not valid for its size.  The loaded
+ * schedules apply to plans built from then on; gl_clear_cache keeps them. */
+int gl_tune_load(const char *path);
+/* Forget every tuned schedule and batch mode: plans built from then on use
+ * the default schedules, GL_BATCH_AUTO the default mode. */
+void gl_tune_clear(void);
 
 /* Fault injection on the host: the next `count` device allocations the
  * library makes for a call's temporaries (scratch, staging, batch blocks)

@@ -1,0 +1,141 @@
+"""Tuned schedules: JSON persistence on the host (gl_tune_save/gl_tune_load)
+and, on the GPU, gl_plan_autotune's measured choice and its parity."""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import from_dev, rand_field, to_dev
+
+
+def _gpu_part(desc):
+    return desc.split(" | gpu: ")[1]
+
+
+@pytest.fixture
+def tuned(gl):
+    """The tuning module; default schedules again after the test."""
+    from goldilocks_gb300 import tune
+    tune.clear()
+    yield tune
+    tune.clear()
+
+
+def test_load_applies_schedule(gl, tuned, tmp_path):
+    before = _gpu_part(gl.strategy(1 << 20).describe())
+    assert before.startswith("col 1024")
+    f = tmp_path / "t.json"
+    f.write_text(json.dumps({"format": "goldilocks-gb300-tuning", "version": 1, "device": "x",
+                             "plans": [{"size": 1 << 20, "kind": 2, "factors": [512, 2048], "lanes": 4}]}))
+    tuned.load(str(f))
+    after = _gpu_part(gl.strategy(1 << 20).describe())
+    assert after.startswith("col 512") and "row 2048" in after and "4 lanes" in after, after
+    # The schedule survives clear_cache: it is a tuned choice, not a cached plan.
+    gl.clear_cache()
+    assert _gpu_part(gl.strategy(1 << 20).describe()) == after
+    # clear() brings the default back.
+    tuned.clear()
+    assert _gpu_part(gl.strategy(1 << 20).describe()) == before
+    # A three-pass schedule of the same size.
+    f.write_text(json.dumps({"format": "goldilocks-gb300-tuning", "version": 1,
+                             "plans": [{"size": 1 << 20, "kind": 3, "factors": [64, 128, 128]}]}))
+    tuned.load(str(f))
+    d = _gpu_part(gl.strategy(1 << 20).describe())
+    assert d.startswith("col 64") and d.count("col") == 2 and "row 128" in d, d
+
+
+def test_save_load_round_trip(gl, tuned, tmp_path):
+    src = {"format": "goldilocks-gb300-tuning", "version": 1,
+           "plans": [{"size": 3 << 16, "kind": 2, "factors": [192, 1024], "lanes": 4, "ms": 0.25}],
+           "batches": [{"mode": "persistent", "polys": [[4096, 1], [1 << 16, 0], [4096, 0]]}]}
+    f = tmp_path / "a.json"
+    f.write_text(json.dumps(src))
+    tuned.load(str(f))
+    out = tmp_path / "b.json"
+    tuned.save(str(out))
+    saved = json.loads(out.read_text())
+    assert saved["format"] == "goldilocks-gb300-tuning" and saved["version"] == 1
+    plans = {p["size"]: p for p in saved["plans"]}
+    p = plans[3 << 16]
+    assert (p["kind"], p["factors"], p["lanes"]) == (2, [192, 1024], 4)
+    assert abs(p["ms"] - 0.25) < 1e-9
+    shapes = {tuple(map(tuple, b["polys"])): b["mode"] for b in saved["batches"]}
+    assert shapes[((4096, 0), (4096, 1), (65536, 0))] == "persistent"  # stored sorted
+    # Loading what was saved gives the same file again.
+    tuned.load(str(out))
+    out2 = tmp_path / "c.json"
+    tuned.save(str(out2))
+    assert json.loads(out2.read_text()) == saved
+
+
+@pytest.mark.parametrize("doc", [
+    "not json",
+    '{"format": "goldilocks-gb300-tuning", "version": 2}',
+    '{"format": "other", "version": 1}',
+    '{"format": "goldilocks-gb300-tuning", "version": 1, "plans": [{"size": 1048576, "kind": 2, '
+    '"factors": [512, 1024]}]}',                                   # product is not the size
+    '{"format": "goldilocks-gb300-tuning", "version": 1, "plans": [{"size": 1048576, "kind": 2, '
+    '"factors": [2, 524288]}]}',                                   # no pass kernel for 524288
+    '{"format": "goldilocks-gb300-tuning", "version": 1, "plans": [{"size": 1048576, "kind": 2, '
+    '"factors": [1024, 1024], "lanes": 3}]}',
+    '{"format": "goldilocks-gb300-tuning", "version": 1, "plans": [{"size": 257, "kind": 1}]}',
+    '{"format": "goldilocks-gb300-tuning", "version": 1, "plans": [{"size": 7, "kind": 1}]}',
+    '{"format": "goldilocks-gb300-tuning", "version": 1, "batches": [{"mode": "fast", '
+    '"polys": [[4096, 0]]}]}',
+    '{"format": "goldilocks-gb300-tuning", "version": 1, "batches": [{"mode": "buckets", '
+    '"polys": [[4096, 2]]}]}',
+    '{"format": "goldilocks-gb300-tuning", "version": 1} trailing',
+    '[' * 100 + ']' * 100,
+])
+def test_invalid_file_changes_nothing(gl, tuned, tmp_path, doc):
+    from goldilocks_gb300 import _lib as L
+    from goldilocks_gb300.ntt import GoldilocksError
+    before = gl.strategy(1 << 20).describe()
+    # A valid entry ahead of the invalid one must not be applied either.
+    if doc.startswith('{"format": "goldilocks-gb300-tuning", "version": 1, "plans": [{'):
+        doc = doc.replace('"plans": [', '"plans": [{"size": 1048576, "kind": 2, "factors": [256, 4096]}, ', 1)
+    f = tmp_path / "bad.json"
+    f.write_text(doc)
+    with pytest.raises(GoldilocksError) as e:
+        tuned.load(str(f))
+    assert e.value.status == L.GL_ERR_INVALID
+    assert gl.strategy(1 << 20).describe() == before
+
+
+def test_io_errors(gl, tuned, tmp_path):
+    from goldilocks_gb300 import _lib as L
+    from goldilocks_gb300.ntt import GoldilocksError
+    with pytest.raises(GoldilocksError) as e:
+        tuned.load(str(tmp_path / "missing.json"))
+    assert e.value.status == L.GL_ERR_IO
+    with pytest.raises(GoldilocksError) as e:
+        tuned.save(str(tmp_path / "no_dir" / "x.json"))
+    assert e.value.status == L.GL_ERR_IO
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [1 << 20, 3 << 18, 17 << 16, 1 << 24])
+def test_autotune_choice_is_exact(gl, cuda, oracle, tuned, n):
+    """Every candidate is checked against the default inside the call; the
+    installed plan then matches the oracle, forward and inverse."""
+    default_ms, chosen_ms = tuned.autotune(n, reps=3)
+    assert 0 < chosen_ms <= default_ms
+    x = rand_field(n, 31)
+    d = to_dev(cuda, x)
+    gl.ntt(d)
+    y = from_dev(d)
+    assert np.array_equal(y, oracle.ntt(x)), gl.strategy(n).describe()
+    gl.intt(d)
+    assert np.array_equal(from_dev(d), x)
+
+
+@pytest.mark.gpu
+def test_autotune_rader_and_single_pass(gl, cuda, oracle, tuned):
+    for n in (257 * 4096, 4096, 1):
+        a, b = tuned.autotune(n, reps=2)
+        assert a >= 0 and b >= 0
+        if n > 1:
+            x = rand_field(n, 5)
+            d = to_dev(cuda, x)
+            gl.ntt(d)
+            assert np.array_equal(from_dev(d), oracle.ntt(x)), gl.strategy(n).describe()
