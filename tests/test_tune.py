@@ -139,3 +139,26 @@ def test_autotune_rader_and_single_pass(gl, cuda, oracle, tuned):
             d = to_dev(cuda, x)
             gl.ntt(d)
             assert np.array_equal(from_dev(d), oracle.ntt(x)), gl.strategy(n).describe()
+
+
+def test_tuning_file_from_environment(gl, tmp_path):
+    """GOLDILOCKS_TUNING names a file loaded before the first plan is built."""
+    import os
+    import subprocess
+    import sys
+    f = tmp_path / "env.json"
+    f.write_text(json.dumps({"format": "goldilocks-gb300-tuning", "version": 1,
+                             "plans": [{"size": 1 << 20, "kind": 2, "factors": [512, 2048], "lanes": 4}]}))
+    code = ("import goldilocks_gb300 as G; "
+            "print(G.strategy(1 << 20).describe().split(' | gpu: ')[1])")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, GOLDILOCKS_TUNING=str(f), PYTHONPATH=root)
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
+                         timeout=120, cwd=root)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.startswith("col 512") and "4 lanes" in out.stdout, out.stdout
+    env["GOLDILOCKS_TUNING"] = str(tmp_path / "missing.json")
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
+                         timeout=120, cwd=root)
+    assert out.returncode == 0 and out.stdout.startswith("col 1024"), out.stdout + out.stderr
+    assert "not loaded" in out.stderr
