@@ -7,6 +7,7 @@ smooth ones, without the factors 17, 257, 65537, unless --all -- and print
   python -m goldilocks_gb300.cli --max-exponent 24 --all       # every divisor
   python -m goldilocks_gb300.cli --algo merkle --max-exponent 24
   python -m goldilocks_gb300.cli --sizes 1048576 --cols 256 --lde 4
+  python -m goldilocks_gb300.cli --max-exponent 26 --tune tuning.json   # tuned schedules
 
 Algorithms (the reference's `--algo`): ntt, inverse, merkle (the K12 tree of
 the size*8 bytes of field elements).  Inputs are device-resident; durations
@@ -28,6 +29,8 @@ def main(argv=None):
     ap.add_argument("--algo", choices=["ntt", "inverse", "merkle"], default="ntt")
     ap.add_argument("--cols", type=int, default=1, help="transform the columns of a rows x cols matrix")
     ap.add_argument("--lde", type=int, default=0, help="coset LDE with this blowup (shift 7)")
+    ap.add_argument("--tune", type=str, default="",
+                    help="autotune each size's schedule first and save the choices to this JSON file")
     args = ap.parse_args(argv)
     if args.inverse:
         args.algo = "inverse"
@@ -77,6 +80,10 @@ def main(argv=None):
             if rc:
                 raise gl.GoldilocksError(rc, "cli")
 
+        if args.tune and args.algo != "merkle":
+            from . import tune
+            tune.autotune(n, reps=max(args.reps, 3))
+            tune.save(args.tune)
         try:
             for _ in range(args.warmup):
                 run()
