@@ -147,10 +147,11 @@ class _Ring:
 def serve_stream(reqs, arrivals, pool, budget_bytes=64 << 30, slots=4, max_batch=64, ring_words=0):
     """Submit each request at its arrival time (seconds from start), wait for
     all; returns (elements/s, stats, wall seconds, outputs).  With ring_words
-    > 0 the outputs share a ring of that many words (no outputs returned)."""
+    > 0 the outputs share a ring of that many words: each returned output is
+    a view of the ring, which a later request may have overwritten."""
     import torch
     if ring_words:
-        ins, outs, ring = [pool[:n * c] for _, n, c, _ in reqs], None, _Ring(torch, ring_words)
+        ins, outs, ring = [pool[:n * c] for _, n, c, _ in reqs], [], _Ring(torch, ring_words)
     else:
         (ins, outs), ring = _buffers(torch, reqs, pool), None
     torch.cuda.synchronize()
@@ -168,6 +169,7 @@ def serve_stream(reqs, arrivals, pool, budget_bytes=64 << 30, slots=4, max_batch
                 time.sleep(a - now)
             if ring:
                 o, lo, hi = ring.take(_out_words(op, n, cols, blowup), wait)
+                outs.append(o)
             else:
                 o = outs[k]
             rid = srv.submit(op, n, cols, i, o, blowup)

@@ -56,3 +56,28 @@ def test_rejections_cancellation_and_bounded_wait(gl, cuda):
             srv.wait(123456789)
         assert e.value.status == L.GL_ERR_NOT_FOUND
         assert srv.stats()["rejected"] == 2
+
+
+def test_ring_outputs_and_full_mix_entry_point(gl, cuda, capsys):
+    """Outputs carved from a ring equal outputs in their own buffers: with a
+    ring that holds every output all of them are compared; with a ring of
+    three outputs (so that the submitter waits for older requests) the last
+    output is.  The full-mix entry point runs end to end on a small case."""
+    import json
+    from goldilocks_gb300 import server as S
+    reqs = S.make_requests(40, seed=21, log_min=6, log_max=14, max_cols=8)
+    pool = to_dev(cuda, gl.fill_uniform(max(n * c for _, n, c, _ in reqs), seed=4))
+    _, _, _, alone = S.serial_baseline(reqs, pool)
+    arrivals = S.poisson_arrivals(len(reqs), rate_per_s=5000.0, seed=21)
+    total = sum(S._out_words(*r) for r in reqs)
+    for ring_words, check in ((total, range(len(reqs))), (3 * max(S._out_words(*r) for r in reqs), [-1])):
+        rate, stats, _, outs = S.serve_stream(reqs, arrivals, pool, budget_bytes=1 << 26, slots=2,
+                                              max_batch=8, ring_words=ring_words)
+        assert rate > 0 and stats["completed"] == len(reqs)
+        for k in check:
+            assert np.array_equal(from_dev(outs[k]), from_dev(alone[k])), (ring_words, k, reqs[k])
+    _, _, _, none = S.serial_baseline(reqs, pool, ring_words=total)
+    assert none is None
+    S.main(["--requests", "30", "--log-max", "12", "--max-cols", "4", "--ring-gib", "1"])
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["requests"] == 30 and len(line["served"]) == 2
