@@ -5,10 +5,10 @@
 // every transform of its op list there, and is copied back once.  A large
 // two-pass transform moves in column blocks (2D copies): its column pass
 // starts on the blocks that have arrived and its last row pass hands output
-// blocks to the copy-out stream as they finish.  Three
-// streams per device -- copy-in, compute, copy-out -- with a ring of `depth`
-// device slots, so job i+1 is copied in while job i computes and job i-1 is
-// copied out.  The host-device link carries both directions at once (on
+// blocks to the copy-out stream as they finish.  Four
+// streams per device -- copy-in, two compute streams, copy-out -- with a
+// ring of `depth` device slots, so job i+1 is copied in while job i computes
+// and job i-1 is copied out.  The host-device link carries both directions at once (on
 // GB300 about 340 GB/s together against about 200 GB/s one way), so the
 // overlap nearly halves the copy time of a plain call per transform.
 #include <algorithm>
@@ -20,8 +20,16 @@
 
 namespace {
 
+// Two compute streams: the main one (high priority) runs the jobs' passes in
+// job order, so that each job's output reaches the copy-out stream as early
+// as possible; the early one (low priority) runs the first, copy-paced column
+// pass of chunked jobs as their blocks arrive, on SMs the main stream leaves
+// idle.  Jobs alternate between two scratch buffers.
+constexpr int kComp = 2;
+
 struct pipe_streams {
-  cudaStream_t in = nullptr, comp = nullptr, out = nullptr;
+  cudaStream_t in = nullptr, out = nullptr;
+  cudaStream_t comp[kComp] = {nullptr, nullptr};
   std::mutex mu;  // one pipeline per device at a time
 };
 
@@ -37,9 +45,14 @@ int streams_for_device(pipe_streams **out) {
   if (it == g_pipes.end()) {
     auto *p = new pipe_streams();
     if ((e = cudaStreamCreateWithFlags(&p->in, cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaStreamCreateWithFlags(&p->comp, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&p->out, cudaStreamNonBlocking)) != cudaSuccess)
       return gl_cuda_status(e);
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    for (int c = 0; c < kComp; c++)
+      if ((e = cudaStreamCreateWithPriority(&p->comp[c], cudaStreamNonBlocking,
+                                            c == 0 ? greatest : least)) != cudaSuccess)
+        return gl_cuda_status(e);
     it = g_pipes.emplace(dev, p).first;
   }
   *out = it->second;
@@ -89,23 +102,28 @@ extern "C" int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_
   std::lock_guard<std::mutex> lk(ps->mu);
   gl_init_mempool_once();
   uint64_t *block = nullptr;
-  const uint64_t words = depth * slot_words + scratch_words;
-  cudaError_t e = gl_malloc_async((void **)&block, std::max<uint64_t>(words, 1) * 8, ps->comp);
+  const int ncomp = njobs > 1 ? kComp : 1;
+  const uint64_t words = depth * slot_words + ncomp * scratch_words;
+  cudaStream_t comp0 = ps->comp[0];
+  cudaError_t e = gl_malloc_async((void **)&block, std::max<uint64_t>(words, 1) * 8, comp0);
   if (e != cudaSuccess) return gl_cuda_status(e);
-  events ready, done, freed, alloc;
+  events ready, done, freed, alloc, col_done;
   if ((st = ready.make(njobs)) != GL_OK || (st = done.make(njobs)) != GL_OK ||
-      (st = freed.make(njobs)) != GL_OK || (st = alloc.make(1)) != GL_OK) {
-    cudaFreeAsync(block, ps->comp);
+      (st = freed.make(njobs)) != GL_OK || (st = alloc.make(1)) != GL_OK ||
+      (st = col_done.make(njobs)) != GL_OK) {
+    cudaFreeAsync(block, comp0);
     return st;
   }
-  cudaEventRecord(alloc.ev[0], ps->comp);  // the block exists for the copy streams
+  cudaEventRecord(alloc.ev[0], comp0);  // the block exists for the other streams
   cudaStreamWaitEvent(ps->in, alloc.ev[0], 0);
-  uint64_t *scratch = block + depth * slot_words;
+  cudaStreamWaitEvent(ps->comp[1], alloc.ev[0], 0);
   std::vector<cudaEvent_t> chunk_ev;  // per chunked job: kChunks copy-ins, then kChunks row passes
   for (uint64_t i = 0; i < njobs && st == GL_OK; i++) {
     const gl_host_job &j = jobs[i];
     gl_plan *pl = plans[i];
     uint64_t *buf = block + (i % depth) * slot_words;
+    cudaStream_t comp = comp0, early = ps->comp[1];
+    uint64_t *scratch = block + depth * slot_words + (i % ncomp) * scratch_words;
     const uint64_t words_i = j.len * j.count;
     if (i >= depth) cudaStreamWaitEvent(ps->in, freed.ev[i - depth], 0);  // slot copied out
     // A large two-pass transform is moved in column blocks: its column pass
@@ -133,26 +151,31 @@ extern "C" int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_
       for (uint32_t k = 0; k < j.nops && st == GL_OK; k++) {
         const bool inv = j.dirs[k] == GL_INVERSE;
         if (k == 0) {
+          // On the early stream, once the job two back (same scratch) is done.
+          cudaStream_t cs = ncomp > 1 ? early : comp;
+          if (ncomp > 1 && i >= 2) cudaStreamWaitEvent(cs, done.ev[i - 2], 0);
           for (int q = 0; q < kChunks && st == GL_OK; q++) {
-            cudaStreamWaitEvent(ps->comp, chunk_ev[base_ev + q], 0);
-            st = gl_enqueue_pass_range(pl, 0, buf, scratch, q * w2, (q + 1) * w2, inv, ps->comp);
+            cudaStreamWaitEvent(cs, chunk_ev[base_ev + q], 0);
+            st = gl_enqueue_pass_range(pl, 0, buf, scratch, q * w2, (q + 1) * w2, inv, cs);
           }
+          cudaEventRecord(col_done.ev[i], cs);
+          cudaStreamWaitEvent(comp, col_done.ev[i], 0);
         } else {
-          st = gl_enqueue_pass_range(pl, 0, buf, scratch, 0, n2, inv, ps->comp);
+          st = gl_enqueue_pass_range(pl, 0, buf, scratch, 0, n2, inv, comp);
         }
         if (st != GL_OK) break;
         if (k + 1 < j.nops) {
-          st = gl_enqueue_pass_range(pl, 1, scratch, buf, 0, n1, inv, ps->comp);
+          st = gl_enqueue_pass_range(pl, 1, scratch, buf, 0, n1, inv, comp);
         } else {
           // output (k2, k1) at k2*n1 + k1: the row pass over rows [r w1, (r+1) w1)
           // writes output column block r
           for (int r = 0; r < kChunks && st == GL_OK; r++) {
-            st = gl_enqueue_pass_range(pl, 1, scratch, buf, r * w1, (r + 1) * w1, inv, ps->comp);
-            cudaEventRecord(chunk_ev[base_ev + kChunks + r], ps->comp);
+            st = gl_enqueue_pass_range(pl, 1, scratch, buf, r * w1, (r + 1) * w1, inv, comp);
+            cudaEventRecord(chunk_ev[base_ev + kChunks + r], comp);
           }
         }
       }
-      cudaEventRecord(done.ev[i], ps->comp);
+      cudaEventRecord(done.ev[i], comp);
       for (int r = 0; r < kChunks && st == GL_OK && e == cudaSuccess; r++) {
         cudaStreamWaitEvent(ps->out, chunk_ev[base_ev + kChunks + r], 0);
         e = cudaMemcpy2DAsync(j.data + r * w1, n1 * 8, buf + r * w1, n1 * 8, w1 * 8, n2,
@@ -166,30 +189,37 @@ extern "C" int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_
       e = cudaMemcpyAsync(buf, j.data, words_i * 8, cudaMemcpyHostToDevice, ps->in);
     if (e != cudaSuccess) { st = gl_cuda_status(e); break; }
     cudaEventRecord(ready.ev[i], ps->in);
-    cudaStreamWaitEvent(ps->comp, ready.ev[i], 0);
+    cudaStreamWaitEvent(comp, ready.ev[i], 0);
     for (uint32_t k = 0; k < j.nops && st == GL_OK && words_i; k++) {
       const bool inv = j.dirs[k] == GL_INVERSE;
       if (inv && j.len <= 1) continue;  // ntt/src/ntt/mod.rs:105-107
-      st = gl_enqueue_transform(pl, buf, buf, 1, j.count, j.len, inv, scratch, ps->comp);
+      st = gl_enqueue_transform(pl, buf, buf, 1, j.count, j.len, inv, scratch, comp);
     }
-    cudaEventRecord(done.ev[i], ps->comp);
+    cudaEventRecord(done.ev[i], comp);
     cudaStreamWaitEvent(ps->out, done.ev[i], 0);
     if (words_i && st == GL_OK)
       e = cudaMemcpyAsync(j.data, buf, words_i * 8, cudaMemcpyDeviceToHost, ps->out);
     if (e != cudaSuccess) st = gl_cuda_status(e);
     cudaEventRecord(freed.ev[i], ps->out);
   }
-  // The block is freed on the compute stream once every copy-out is done.
-  cudaEvent_t last = nullptr;
-  if (cudaEventCreateWithFlags(&last, cudaEventDisableTiming) == cudaSuccess) {
-    cudaEventRecord(last, ps->out);
-    cudaStreamWaitEvent(ps->comp, last, 0);
+  // The block is freed on the first compute stream once every copy-out and
+  // the other compute stream are done.
+  cudaEvent_t last[kComp] = {nullptr, nullptr};
+  for (int c = 0; c < kComp; c++) {
+    if (cudaEventCreateWithFlags(&last[c], cudaEventDisableTiming) != cudaSuccess) { last[c] = nullptr; continue; }
+    cudaEventRecord(last[c], c == 0 ? ps->out : ps->comp[c]);
+    cudaStreamWaitEvent(comp0, last[c], 0);
   }
-  cudaFreeAsync(block, ps->comp);
+  cudaFreeAsync(block, comp0);
   cudaError_t e1 = cudaStreamSynchronize(ps->in);
   cudaError_t e2 = cudaStreamSynchronize(ps->out);
-  cudaError_t e3 = cudaStreamSynchronize(ps->comp);
-  if (last) cudaEventDestroy(last);
+  cudaError_t e3 = cudaSuccess;
+  for (int c = 0; c < kComp; c++) {
+    const cudaError_t ec = cudaStreamSynchronize(ps->comp[c]);
+    if (e3 == cudaSuccess) e3 = ec;
+  }
+  for (int c = 0; c < kComp; c++)
+    if (last[c]) cudaEventDestroy(last[c]);
   for (auto ev : chunk_ev) cudaEventDestroy(ev);
   if (st != GL_OK) return st;
   if (e1 != cudaSuccess) return gl_cuda_status(e1);
