@@ -207,6 +207,26 @@ def bench_batched(gl, torch, reps=3):
         b.synchronize()
         out[name + "_elem_s"] = out["elements"] * reps / (a.elapsed_time(b) * 1e-3)
     out["persistent_vs_per_call"] = out["persistent_elem_s"] / out["per_call_elem_s"]
+    # The schedules of the batch's lengths measured first (gl_plan_autotune),
+    # then buckets again, and AUTO with the mode gl_batch_autotune measured.
+    from goldilocks_gb300 import tune
+    try:
+        for n in sorted(set(sizes)):
+            tune.autotune(n, reps=10)
+        for name, mode in (("buckets_tuned", B.BUCKETS), ("auto_tuned", B.AUTO)):
+            if mode == B.AUTO:
+                B.autotune(items, reps=2)
+            B.run(items, mode=mode)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                B.run(items, mode=mode)
+            b.record(stream)
+            b.synchronize()
+            out[name + "_elem_s"] = out["elements"] * reps / (a.elapsed_time(b) * 1e-3)
+    finally:
+        tune.clear()
     return out
 
 

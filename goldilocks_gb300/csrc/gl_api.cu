@@ -683,6 +683,11 @@ void gl_launch(const gl_kernel_entry *k, int role, const gl_pass_args &a0, dim3 
   if (k->generic) { a.gen_r[0] = k->r1; a.gen_r[1] = k->r2; a.gen_r[2] = k->r3; }
   bool on;
   on = g_prof_on.load(std::memory_order_relaxed);
+  // Launches captured into a CUDA graph are not bracketed: the graph would
+  // keep event nodes for events the profile destroys when it is reset.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (on && cudaStreamIsCapturing(stream, &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone)
+    on = false;
   if (!on) { k->launch(a, grid, stream); return; }
   gl_prof_rec r{k, role, elements, nullptr, nullptr};
   cudaEventCreate(&r.a);

@@ -349,6 +349,11 @@ struct bucket_graph {
   void *tables = nullptr;                  // pointer tables (device)
   size_t table_words = 0;
   std::vector<std::pair<uint64_t, int>> sig;  // (len, dir) per item, bucket order
+  std::vector<const gl_plan *> plans;         // the plan of each item when captured
+  ~bucket_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (tables) cudaFree(tables);
+  }
 };
 
 std::mutex g_graph_mu;
@@ -387,13 +392,26 @@ int run_buckets(const gl_poly *polys, uint64_t count, const std::vector<poly_pla
     flat[j] = polys[order[j]].data;
     flat[nitems + j] = (uint64_t *)scr.p + scr_off[j];
   }
+  std::vector<const gl_plan *> plans(nitems);
+  for (size_t j = 0; j < nitems; j++) plans[j] = pp[order[j]].pl;
   std::lock_guard<std::mutex> lk(g_graph_mu);
   auto &slot = g_graphs[sig];
+  if (slot && slot->plans != plans) {
+    // A schedule of one of the sizes changed (tuned or loaded) since the
+    // capture: capture again with the current plans.
+    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return gl_cuda_status(e);
+    slot.reset();
+  }
   if (!slot) {
     auto g = std::make_unique<bucket_graph>();
     g->sig = sig;
+    g->plans = plans;
     g->table_words = flat.size();
-    if ((e = cudaMalloc(&g->tables, flat.size() * sizeof(void *))) != cudaSuccess) return gl_cuda_status(e);
+    if ((e = cudaMalloc(&g->tables, flat.size() * sizeof(void *))) != cudaSuccess) {
+      g->tables = nullptr;
+      g_graphs.erase(sig);
+      return gl_cuda_status(e);
+    }
     uint64_t **dt = (uint64_t **)g->tables;
     cudaStream_t cap;
     if ((e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking)) != cudaSuccess) return gl_cuda_status(e);
@@ -434,8 +452,7 @@ int run_buckets(const gl_poly *polys, uint64_t count, const std::vector<poly_pla
     if (e2 == cudaSuccess) cudaGraphDestroy(graph);
     cudaStreamDestroy(cap);
     if (e != cudaSuccess) {
-      cudaFree(g->tables);
-      g_graphs.erase(sig);
+      g_graphs.erase(sig);  // g frees its tables
       return gl_cuda_status(e);
     }
     slot = std::move(g);

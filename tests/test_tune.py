@@ -162,3 +162,30 @@ def test_tuning_file_from_environment(gl, tmp_path):
                          timeout=120, cwd=root)
     assert out.returncode == 0 and out.stdout.startswith("col 1024"), out.stdout + out.stderr
     assert "not loaded" in out.stderr
+
+
+@pytest.mark.gpu
+def test_bucket_batches_after_a_schedule_change(gl, cuda, oracle, tuned, tmp_path):
+    """A batch replayed from a captured CUDA graph stays exact when the
+    schedule of its length changes after the capture (two-pass split and lane
+    width, then a three-pass schedule, which runs per call)."""
+    from goldilocks_gb300 import batch as B
+    n = 1 << 14
+    xs = [rand_field(n, 100 + i) for i in range(8)]
+    want = [oracle.ntt(x) if i % 2 == 0 else oracle.intt(x) for i, x in enumerate(xs)]
+
+    def run():
+        ds = [to_dev(cuda, x) for x in xs]
+        B.run([(d, B.FORWARD if i % 2 == 0 else B.INVERSE) for i, d in enumerate(ds)], mode=B.BUCKETS)
+        for i, d in enumerate(ds):
+            assert np.array_equal(from_dev(d), want[i]), (i, gl.strategy(n).describe())
+
+    run()
+    run()  # replayed from the graph
+    f = tmp_path / "t.json"
+    for plan in ({"size": n, "kind": 2, "factors": [64, 256], "lanes": 4},
+                 {"size": n, "kind": 3, "factors": [16, 32, 32]}):
+        f.write_text(json.dumps({"format": "goldilocks-gb300-tuning", "version": 1, "plans": [plan]}))
+        tuned.load(str(f))
+        run()
+        run()
