@@ -108,13 +108,17 @@ class Gen:
         return self.cooley_tukey(xs, a, b)
 
     def dft3(self, xs):
-        # omega_3 = 2^64, omega_3^2 = -2^32 (inverse swaps the two).
+        # One product instead of four: with w = omega_3 (2^64; the inverse
+        # uses w^2 = -2^32) and w^2 = -1 - w,
+        #   X1 = a + w b + w^2 c = (a - c) + w (b - c)
+        #   X2 = a + w^2 b + w c = (a - b) - w (b - c).
+        # The same field values as the reference's naive form
+        # (ntt/src/bin/codegen.rs), in 7 additions and 1 product.
         a, b, c = xs
-        w1 = lambda v: self.twiddle(v, 3, 1)
-        w2 = lambda v: self.twiddle(v, 3, 2)
         x0 = self.add(self.add(a, b), c)
-        x1 = self.add(self.add(a, w1(b)), w2(c))
-        x2 = self.add(self.add(a, w2(b)), w1(c))
+        m = self.twiddle(self.sub(b, c), 3, 1)
+        x1 = self.add(self.sub(a, c), m)
+        x2 = self.sub(self.sub(a, b), m)
         return [x0, x1, x2]
 
     def cooley_tukey(self, xs, a, b):
