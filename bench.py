@@ -10,8 +10,13 @@ Metric: elements transformed per second (each transform counts n).
              each step, L2 flushed (256 MiB write) between steps outside the
              timed events.
   e2e        the same step through the public API with pinned HOST buffers
-             (gl_ntt/gl_intt with GL_MEM_HOST: H2D copy, kernels, D2H copy and
-             synchronisation inside the timed region).
+             (gl_host_pipeline: one copy in and one copy out per buffer,
+             overlapped with the transforms, synchronised, inside the timed
+             region); e2e.per_call: one synchronous gl_plan_execute with
+             GL_MEM_HOST per transform.
+  issue_roofline  the same kernel against the instruction-issue peak (the
+             bound these integer kernels meet), from the ncu instruction count
+             per element.
   roofline   the kernel with the largest share of device time, its algorithmic
              bytes per launch (16 B per element per pass: one read + one write)
              over its mean CUDA-event launch time, against the measured HBM
@@ -126,13 +131,19 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def ncu_traffic():
-    """Per-element DRAM traffic of each kernel from the committed ncu summary."""
+def ncu_per_element(name):
+    """Per-element figures of each kernel from the committed ncu summary:
+    ncu_traffic.json (DRAM bytes read + written), ncu_inst.json (thread
+    instructions executed)."""
     try:
-        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+        with open(os.path.join(ROOT, "profiles", name)) as f:
             return json.load(f)
     except Exception:
         return {}
+
+
+def ncu_traffic():
+    return ncu_per_element("ncu_traffic.json")
 
 
 def cpu_oracle_step(threads):
@@ -504,6 +515,22 @@ def run_ours(args):
                     "algorithmic_bytes_per_launch": 16.0 * per_launch_el,
                     "mean_launch_ms": mean_ms,
                     "share": dom["total_ms"] / max(sum(p["total_ms"] for p in prof), 1e-12)}
+    # The bound the passes actually meet: instruction issue (4 warp
+    # instructions per SM per clock), from the ncu instruction count per
+    # element and the live launch time, at the SM clock sampled during the run.
+    issue = None
+    inst = ncu_per_element("ncu_inst.json").get(dom["name"]) if dom else None
+    if inst and clk and clk.get("sm_mhz"):
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        per_launch_el = dom["elements"] / dom["launches"]
+        mean_s = dom["total_ms"] / dom["launches"] * 1e-3
+        achieved_i = inst / 32.0 * per_launch_el / mean_s / 1e9
+        peak_i = sms * 4 * clk["sm_mhz"] * 1e6 / 1e9
+        issue = {"bound": "integer issue", "kernel": dom["name"], "inst_per_element": inst,
+                 "achieved": achieved_i, "peak": peak_i, "unit": "G warp-instructions/s",
+                 "frac": achieved_i / peak_i,
+                 "basis": "thread instructions per element from the committed ncu capture; "
+                          "4 warp instructions per SM per clock at the sampled SM clock"}
     # whole-transform roofline: 16 B * n * passes(n) per transform, passes = ceil(log2 n / 14)
     import math
     alg_bytes = sum(2 * 16 * n * math.ceil(math.log2(n) / 14) for n in SIZES)
@@ -514,6 +541,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "u64 (mod p)", "data": "synthetic",
             "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single GPU"),
             "roofline": roofline,
+            "issue_roofline": issue,
             "step_roofline": {"algorithmic_bytes_per_step": alg_bytes,
                               "achieved_gbs": alg_bytes / (step_ms * 1e-3) / 1e9,
                               "frac": alg_bytes / (step_ms * 1e-3) / 1e9 / peak},
