@@ -388,13 +388,14 @@ std::vector<std::pair<uint64_t, gl_choice>> gl_tuned_list() {
 }
 
 // GOLDILOCKS_TUNING=<file>: schedules and batch modes a gl_tune_save wrote,
-// loaded before the first plan is built.
-static void autoload_tuning() {
+// loaded before the first plan is built and before any explicit tuning call
+// (gl_tune_load, gl_tune_clear, gl_plan_autotune), which then take precedence.
+void gl_tune_autoload() {
   static std::once_flag once;
   std::call_once(once, [] {
     const char *path = getenv("GOLDILOCKS_TUNING");
     if (!path || !*path) return;
-    const int st = gl_tune_load(path);
+    const int st = gl_tune_load_file(path);
     if (st != GL_OK) fprintf(stderr, "goldilocks: GOLDILOCKS_TUNING=%s not loaded: %s\n", path, gl_status_string(st));
   });
 }
@@ -402,7 +403,7 @@ static void autoload_tuning() {
 // The tuned schedule of the size if one was measured or loaded, else the
 // default.
 static void choose_schedule(gl_plan *pl) {
-  autoload_tuning();
+  gl_tune_autoload();
   gl_choice c = gl_choice_default(pl->size);
   {
     std::lock_guard<std::mutex> lk(g_tuned_mu);

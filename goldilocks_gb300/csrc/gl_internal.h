@@ -226,6 +226,10 @@ void gl_plan_install(gl_plan *pl);
 // Drop every cached plan of size n (and the Rader plans); the next
 // gl_plan_create builds it again.
 void gl_plan_forget(uint64_t n);
+// Loads the GOLDILOCKS_TUNING file once (gl_api.cu) through
+// gl_tune_load_file (gl_tune.cu), which applies one file's entries.
+void gl_tune_autoload();
+int gl_tune_load_file(const char *path);
 
 // Tuned batch modes per batch shape (sorted (length, direction) pairs).
 // (gl_batch.cu)

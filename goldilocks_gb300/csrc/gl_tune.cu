@@ -147,6 +147,7 @@ int autotune_rader(gl_plan *cur, int reps, cudaStream_t s, double *ms_out) {
 
 extern "C" int gl_plan_autotune(uint64_t size, int reps, void *stream_, double *ms_out) {
   GL_NVTX("gl_plan_autotune");
+  gl_tune_autoload();
   cudaStream_t s = (cudaStream_t)stream_;
   if (reps <= 0) return GL_ERR_INVALID;
   if (!gl_is_divisor(size)) return GL_ERR_UNSUPPORTED_SIZE;
@@ -511,8 +512,9 @@ extern "C" int gl_tune_save(const char *path) {
   return GL_OK;
 }
 
-extern "C" int gl_tune_load(const char *path) {
-  if (!path) return GL_ERR_INVALID;
+// Applies the entries of one file (gl_tune_load and the GOLDILOCKS_TUNING
+// file).
+static int load_file(const char *path) {
   FILE *fp = fopen(path, "rb");
   if (!fp) return GL_ERR_IO;
   std::string text;
@@ -561,7 +563,16 @@ extern "C" int gl_tune_load(const char *path) {
   return GL_OK;
 }
 
+int gl_tune_load_file(const char *path) { return path ? load_file(path) : GL_ERR_INVALID; }
+
+extern "C" int gl_tune_load(const char *path) {
+  if (!path) return GL_ERR_INVALID;
+  gl_tune_autoload();
+  return load_file(path);
+}
+
 extern "C" void gl_tune_clear(void) {
+  gl_tune_autoload();
   for (const auto &pc : gl_tuned_list()) gl_plan_forget(pc.first);
   gl_tuned_clear();
   gl_batch_tuned_clear();

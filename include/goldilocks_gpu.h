@@ -253,6 +253,9 @@ int gl_tune_load(const char *path);
 /* Forget every tuned schedule and batch mode: plans built from then on use
  * the default schedules, GL_BATCH_AUTO the default mode. */
 void gl_tune_clear(void);
+/* GOLDILOCKS_TUNING=<file> in the environment: that file is loaded once,
+ * before the first plan is built or the first of gl_plan_autotune,
+ * gl_tune_load and gl_tune_clear runs, so explicit calls take precedence. */
 
 /* Fault injection on the host: the next `count` device allocations the
  * library makes for a call's temporaries (scratch, staging, batch blocks)

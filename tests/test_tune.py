@@ -189,3 +189,24 @@ def test_bucket_batches_after_a_schedule_change(gl, cuda, oracle, tuned, tmp_pat
         tuned.load(str(f))
         run()
         run()
+
+
+def test_explicit_calls_take_precedence_over_the_environment_file(gl, tmp_path):
+    """The GOLDILOCKS_TUNING file is applied before an explicit load or clear,
+    whichever comes first in the process."""
+    import os
+    import subprocess
+    import sys
+    env_file, own = tmp_path / "env.json", tmp_path / "own.json"
+    for path, split in ((env_file, [256, 4096]), (own, [512, 2048])):
+        path.write_text(json.dumps({"format": "goldilocks-gb300-tuning", "version": 1,
+                                    "plans": [{"size": 1 << 20, "kind": 2, "factors": split}]}))
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, GOLDILOCKS_TUNING=str(env_file), PYTHONPATH=root)
+    show = "print(G.strategy(1 << 20).describe().split(' | gpu: ')[1])"
+    for code, want in (("T.load(%r)" % str(own), "col 512"), ("T.clear()", "col 1024"), ("pass", "col 256")):
+        prog = "import goldilocks_gb300 as G; from goldilocks_gb300 import tune as T; %s; %s" % (code, show)
+        out = subprocess.run([sys.executable, "-c", prog], env=env, capture_output=True, text=True,
+                             timeout=120, cwd=root)
+        assert out.returncode == 0, out.stderr
+        assert out.stdout.startswith(want), (code, out.stdout)
