@@ -77,13 +77,24 @@ def build(verbose=False, jobs=None):
             o, c = f.result()
             objs.append(o)
             changed |= c
-    if changed or not os.path.exists(LIB):
+    # The set of units is part of the link's inputs (a removed source must
+    # leave the library too).
+    link_stamp = os.path.join(BUILD, "link.stamp")
+    units = "\n".join(objs)
+    try:
+        with open(link_stamp) as f:
+            same_units = f.read() == units
+    except OSError:
+        same_units = False
+    if changed or not same_units or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
         cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
         os.replace(tmp, LIB)
+        with open(link_stamp, "w") as f:
+            f.write(units)
     return LIB
 
 

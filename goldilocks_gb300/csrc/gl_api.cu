@@ -120,17 +120,6 @@ static std::string reference_tree(uint64_t size) {
 
 // ----------------------------------------------------------- kernel lookup
 
-// GOLDILOCKS_PASS_KERNELS=wide selects the two-round kernels (64 elements
-// per thread) for the four-step passes where one exists; the default is the
-// three-round radix-16 kernels.
-static bool use_wide_kernels() {
-  static const bool wide = [] {
-    const char *v = getenv("GOLDILOCKS_PASS_KERNELS");
-    return v && strcmp(v, "wide") == 0;
-  }();
-  return wide;
-}
-
 static const gl_kernel_entry *find_in(const gl_kernel_entry *e, size_t cnt, uint64_t m) {
   for (size_t i = 0; i < cnt; i++)
     if ((uint64_t)e[i].m == m) return &e[i];
@@ -207,10 +196,6 @@ const gl_kernel_entry *gl_find_kernel_cols(uint64_t m, bool inv) {
 
 const gl_kernel_entry *gl_find_kernel4(uint64_t m, bool inv) {
   size_t cnt = 0;
-  if (use_wide_kernels()) {
-    const gl_kernel_entry *e = inv ? gl_kernels_wide_inv(&cnt) : gl_kernels_wide_fwd(&cnt);
-    if (const gl_kernel_entry *k = find_in(e, cnt, m)) return k;
-  }
   const gl_kernel_entry *e = inv ? gl_kernels_pass_inv(&cnt) : gl_kernels_pass_fwd(&cnt);
   if (const gl_kernel_entry *k = find_in(e, cnt, m)) return k;
   return generic_entry(m, inv);  // every other size up to 4096 with radices <= 17

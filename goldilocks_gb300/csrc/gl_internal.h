@@ -31,8 +31,8 @@ cudaError_t gl_malloc_async(void **p, size_t bytes, cudaStream_t stream);
 typedef void (*gl_launch_fn)(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
 
 // One compiled instance of a pass kernel: gl_pass3_kernel (radices r1 x r2 x
-// r3, up to three register rounds) or the two-round gl_pass_kernel (r3 = 0,
-// ma x mb with ma elements per thread).
+// r3, up to three register rounds), or the run-time-radix gl_generic_kernel
+// (generic = true; the radices are passed at launch).
 struct gl_kernel_entry {
   int m, r1, r2, r3, lanes;
   bool inv;
@@ -52,10 +52,6 @@ const gl_kernel_entry *gl_kernels_pass_inv(size_t *count);
 // Passes up to 2048 points with two lanes per CTA and four CTAs per SM.
 const gl_kernel_entry *gl_kernels_pass2_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_pass2_inv(size_t *count);
-// Two-round kernels with up to 64 elements per thread (an alternative the
-// autotuner may choose).
-const gl_kernel_entry *gl_kernels_wide_fwd(size_t *count);
-const gl_kernel_entry *gl_kernels_wide_inv(size_t *count);
 
 // Run-time-radix kernels (gl_kern_generic.cu).
 void gl_launch_generic_fwd(const gl_pass_args &args, dim3 grid, cudaStream_t stream);

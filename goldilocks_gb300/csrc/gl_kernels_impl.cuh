@@ -3,15 +3,6 @@
 #pragma once
 #include "gl_internal.h"
 
-template <int MA, int MB, int LANES, bool INV>
-static void gl_launch_pass(const gl_pass_args &args, dim3 grid, cudaStream_t stream) {
-  constexpr size_t smem = gl_pass_smem_bytes<MA, MB>(LANES);
-  auto kern = gl_pass_kernel<MA, MB, LANES, INV>;
-  static std::atomic<uint64_t> optin{0};
-  gl_smem_optin(optin, kern, smem);
-  kern<<<grid, LANES * MB, smem, stream>>>(args);
-}
-
 template <int R1, int R2, int R3, int LANES, int NT, bool INV, int MINB = 1>
 static void gl_launch_pass3(const gl_pass_args &args, dim3 grid, cudaStream_t stream) {
   constexpr size_t smem = gl_p3_smem_bytes<R1, R2, R3, LANES>();
@@ -20,9 +11,6 @@ static void gl_launch_pass3(const gl_pass_args &args, dim3 grid, cudaStream_t st
   gl_smem_optin(optin, kern, smem);
   kern<<<grid, NT, smem, stream>>>(args);
 }
-
-#define GL_ENTRY(MA, MB, LANES, INV) \
-  {MA * MB, MA, MB, 0, LANES, INV, gl_pass_smem_bytes<MA, MB>(LANES), LANES * MB, gl_launch_pass<MA, MB, LANES, INV>}
 
 #define GL_ENTRY3(R1, R2, R3, LANES, NT, INV)                                                 \
   {R1 * R2 * R3, R1, R2, R3, LANES, INV, gl_p3_smem_bytes<R1, R2, R3, LANES>(), NT,          \

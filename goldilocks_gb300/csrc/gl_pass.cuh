@@ -1,14 +1,10 @@
-// The block-DFT pass kernel: every CTA transforms LANES independent m-point
-// sequences ("lanes") held in one tile, m = MA * MB, as two register rounds
-// with one shared-memory exchange between them:
+// Shared parts of the pass kernels (gl_pass3.cuh, gl_generic.cuh and the
+// persistent batch kernel): the argument block, the debug-checked memory
+// accesses and the twiddle lookups.
 //
-//   j = MB*jA + jB,  k = kA + MA*kB
-//   round 1: per (lane, jB)  Y[kA][jB] = DFT_MA over jA of x[MB*jA + jB]
-//   twiddle:                 Y[kA][jB] *= omega_m^(jB*kA)
-//   round 2: per (lane, kA)  X[kA + MA*kB] = DFT_MB over jB of Y[kA][jB]
-//
-// Strides place the lanes and indices anywhere in memory, so one kernel serves
-// every role of the four-step schedule:
+// A pass transforms LANES independent m-point sequences ("lanes") per CTA.
+// Strides place the lanes and indices anywhere in memory, so one kernel
+// serves every role of the four-step schedule:
 //   COL  pass 1 of a four-step n = n1*n2: lanes are adjacent columns of the
 //        n1 x (n2*C) row-major view, transforms run down the columns, outputs
 //        are multiplied by omega_n^(col*k) with col = lane / C;
@@ -128,132 +124,4 @@ __device__ __forceinline__ uint64_t gl_out_mul(const gl_pass_args &a, const uint
 
 __device__ __forceinline__ uint64_t gl_tw2(const uint64_t *lo, const uint64_t *hi, uint64_t e) {
   return gl_mul(lo[e & 4095], hi[e >> 12]);
-}
-
-template <int MA, int MB>
-struct gl_tile_layout {
-  static constexpr bool POW2 = (MB & (MB - 1)) == 0;
-  // Row stride of the [kA][jB] tile: power-of-two rows are XOR-swizzled,
-  // other even rows are padded by one word to spread banks.
-  static constexpr int RS = POW2 ? MB : (MB % 2 == 0 ? MB + 1 : MB);
-  static constexpr int SWZ = POW2 ? (MB < 16 ? MB - 1 : 15) : 0;
-  // Lane stride = 4 (mod 16) words so that 4 lanes x 4 rows of a half-warp
-  // land on distinct banks.
-  static constexpr int LS = ((MA * RS + 15) / 16) * 16 + 4;
-  static __device__ __forceinline__ int word(int c, int kA, int jB) {
-    return c * LS + kA * RS + (POW2 ? (jB ^ (kA & SWZ)) : jB);
-  }
-};
-
-template <int MA, int MB, int LANES, bool INV>
-__global__ void __launch_bounds__(LANES * MB)
-gl_pass_kernel(const gl_pass_args a) {
-  constexpr int T = LANES * MB;
-  using L = gl_tile_layout<MA, MB>;
-  extern __shared__ uint64_t sm[];
-
-  const int t = threadIdx.x;
-  const int64_t lane0 = (int64_t)blockIdx.x * LANES;
-  const uint64_t *in = a.in + (int64_t)blockIdx.y * a.in_bs + (int64_t)blockIdx.z * a.in_bs2;
-  uint64_t *out = a.out + (int64_t)blockIdx.y * a.out_bs + (int64_t)blockIdx.z * a.out_bs2;
-  const bool scale_all = (a.flags & GL_PF_SCALE_ALL) != 0;
-
-  // ---- round 1: DFT_MA over jA for one (lane, jB) ----
-  int c, jB;
-  if (a.flags & GL_PF_LOAD_LANE_FAST) { c = t % LANES; jB = t / LANES; }
-  else { jB = t % MB; c = t / MB; }
-  const bool live = lane0 + c < (int64_t)a.lanes;
-  uint64_t x[MA];
-  {
-    const uint64_t *src = in + (lane0 + c) * a.in_ls + (int64_t)jB * a.in_is;
-#pragma unroll
-    for (int jA = 0; jA < MA; jA++) {
-      const uint32_t j = (uint32_t)(MB * jA + jB);
-      x[jA] = (live && j < a.in_limit) ? src[(int64_t)(MB * jA) * a.in_is] : 0;
-    }
-    if ((a.flags & (GL_PF_CANON_IN | GL_PF_IN_TWIDDLE)) == GL_PF_CANON_IN) {
-#pragma unroll
-      for (int jA = 0; jA < MA; jA++) x[jA] = gl_canon(x[jA]);
-    }
-    if (a.flags & GL_PF_IN_TWIDDLE) {
-      const uint64_t col = (uint64_t)(lane0 + c) / a.tw_lane_div;
-#pragma unroll
-      for (int jA = 0; jA < MA; jA++) {
-        const uint64_t j = (uint64_t)(MB * jA + jB);
-        if (j < a.in_limit) x[jA] = gl_mont_mul(x[jA], gl_tw2m(a.itw_lo, a.itw_hi, j * a.itw_jmul + col));
-      }
-    }
-  }
-  gl_dft<MA, INV>(x);
-  if constexpr (MB > 1) {
-#pragma unroll
-    for (int kA = 0; kA < MA; kA++)
-      if (kA > 0 || scale_all) x[kA] = gl_mont_mul(x[kA], a.tw_m[jB * kA]);
-  } else if (scale_all) {
-    const uint64_t s = a.tw_m[0];
-#pragma unroll
-    for (int kA = 0; kA < MA; kA++) x[kA] = gl_mont_mul(x[kA], s);
-  }
-
-  if constexpr (MB == 1) {
-    // Single round: kA is the output index.
-    if (live) {
-      uint64_t *dst = out + (lane0 + c) * a.out_ls;
-      if (a.flags & GL_PF_PASS_TWIDDLE) {
-        const uint64_t col = (uint64_t)(lane0 + c) / a.tw_lane_div;
-#pragma unroll
-        for (int kA = 0; kA < MA; kA++)
-          dst[(int64_t)kA * a.out_is] = gl_mont_mul(x[kA], gl_pass_tw(a, col, kA));
-      } else if (a.flags & GL_PF_OUT_MUL) {
-        const uint64_t *mb = a.mul + blockIdx.y * a.mul_bs + blockIdx.z * a.mul_bs2;
-#pragma unroll
-        for (int kA = 0; kA < MA; kA++)
-          dst[(int64_t)kA * a.out_is] = gl_out_mul(a, mb, lane0 + c, kA, x[kA]);
-      } else {
-#pragma unroll
-        for (int kA = 0; kA < MA; kA++) dst[(int64_t)kA * a.out_is] = x[kA];
-      }
-    }
-    return;
-  } else {
-#pragma unroll
-    for (int kA = 0; kA < MA; kA++) sm[L::word(c, kA, jB)] = x[kA];
-    __syncthreads();
-
-    // ---- round 2: DFT_MB over jB for one (lane, kA) ----
-    for (int g = t; g < LANES * MA; g += T) {
-      int c2, kA;
-      if (a.flags & GL_PF_STORE_LANE_FAST) { c2 = g % LANES; kA = g / LANES; }
-      else { kA = g % MA; c2 = g / MA; }
-      const int64_t lane = lane0 + c2;
-      uint64_t y[MB];
-#pragma unroll
-      for (int j = 0; j < MB; j++) y[j] = sm[L::word(c2, kA, j)];
-      gl_dft<MB, INV>(y);
-      if (lane < (int64_t)a.lanes) {
-        uint64_t *dst = out + lane * a.out_ls;
-        if (a.flags & GL_PF_PASS_TWIDDLE) {
-          const uint64_t col = (uint64_t)lane / a.tw_lane_div;
-#pragma unroll
-          for (int kB = 0; kB < MB; kB++) {
-            const uint64_t k = (uint64_t)(kA + MA * kB);
-            dst[(int64_t)k * a.out_is] = gl_mont_mul(y[kB], gl_pass_tw(a, col, k));
-          }
-        } else if (a.flags & GL_PF_OUT_MUL) {
-          const uint64_t *mb = a.mul + blockIdx.y * a.mul_bs + blockIdx.z * a.mul_bs2;
-#pragma unroll
-          for (int kB = 0; kB < MB; kB++)
-            dst[(int64_t)(kA + MA * kB) * a.out_is] = gl_out_mul(a, mb, lane, kA + MA * kB, y[kB]);
-        } else {
-#pragma unroll
-          for (int kB = 0; kB < MB; kB++) dst[(int64_t)(kA + MA * kB) * a.out_is] = y[kB];
-        }
-      }
-    }
-  }
-}
-
-template <int MA, int MB>
-constexpr size_t gl_pass_smem_bytes(int lanes) {
-  return MB == 1 ? 0 : (size_t)lanes * gl_tile_layout<MA, MB>::LS * sizeof(uint64_t);
 }
