@@ -8,6 +8,7 @@ smooth ones, without the factors 17, 257, 65537, unless --all -- and print
   python -m goldilocks_gb300.cli --algo merkle --max-exponent 24
   python -m goldilocks_gb300.cli --sizes 1048576 --cols 256 --lde 4
   python -m goldilocks_gb300.cli --max-exponent 26 --tune tuning.json   # tuned schedules
+  python -m goldilocks_gb300.cli --batch 1024 --batch-mode persistent     # uneven batches
 
 Algorithms (the reference's `--algo`): ntt, inverse, merkle (the K12 tree of
 the size*8 bytes of field elements).  Inputs are device-resident; durations
@@ -29,6 +30,9 @@ def main(argv=None):
     ap.add_argument("--algo", choices=["ntt", "inverse", "merkle"], default="ntt")
     ap.add_argument("--cols", type=int, default=1, help="transform the columns of a rows x cols matrix")
     ap.add_argument("--lde", type=int, default=0, help="coset LDE with this blowup (shift 7)")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="time batches of this many polynomials, log2 n uniform in [12, 18] (seeded)")
+    ap.add_argument("--batch-mode", choices=["auto", "persistent", "buckets", "per_call"], default="auto")
     ap.add_argument("--tune", type=str, default="",
                     help="autotune each size's schedule first and save the choices to this JSON file")
     args = ap.parse_args(argv)
@@ -42,6 +46,8 @@ def main(argv=None):
     from goldilocks_gb300 import _lib as L
 
     lib = L.load()
+    if args.batch:
+        return _run_batch(args, gl, torch, np)
     if args.sizes:
         sizes = [int(s) for s in args.sizes.split(",")]
     else:
@@ -101,6 +107,35 @@ def main(argv=None):
         t = statistics.median(times)
         print("%d,%d,%.9f,%.6e" % (n, args.cols, t, n * args.cols / t))
         sys.stdout.flush()
+    return 0
+
+
+def _run_batch(args, gl, torch, np):
+    """Batches of uneven lengths (gl_batch_execute): one line with the batch
+    time and elements/s.  Odd-indexed polynomials are inverse transforms."""
+    from . import batch as B
+    rng = np.random.default_rng(0xBA7C)
+    sizes = [1 << int(k) for k in rng.integers(12, 19, args.batch)]
+    pool = torch.from_numpy(gl.fill_uniform(sum(sizes), seed=0xBA7C).view(np.int64)).cuda()
+    items, off = [], 0
+    for i, n in enumerate(sizes):
+        items.append((pool[off:off + n], B.INVERSE if i % 2 else B.FORWARD))
+        off += n
+    mode = {"auto": B.AUTO, "persistent": B.PERSISTENT, "buckets": B.BUCKETS, "per_call": B.PER_CALL}[args.batch_mode]
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        B.run(items, mode=mode)
+    times = []
+    for _ in range(args.reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        B.run(items, mode=mode)
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b) * 1e-3)
+    t = statistics.median(times)
+    print("polys,mode,elements,duration,throughput")
+    print("%d,%s,%d,%.9f,%.6e" % (len(sizes), args.batch_mode, sum(sizes), t, sum(sizes) / t))
     return 0
 
 
