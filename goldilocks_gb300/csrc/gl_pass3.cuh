@@ -18,7 +18,7 @@
 #pragma once
 #include "gl_pass.cuh"
 
-template <int R1, int R2, int R3>
+template <int R1, int R2, int R3, int LANES>
 struct gl_p3_layout {
   static constexpr int M = R1 * R2 * R3;
   static constexpr int NR = R2 == 1 ? 1 : (R3 == 1 ? 2 : 3);
@@ -26,8 +26,14 @@ struct gl_p3_layout {
   static constexpr bool POW2 = (RL & (RL - 1)) == 0 && (M & (M - 1)) == 0;
   static constexpr int SH = RL == 16 ? 4 : RL == 8 ? 3 : RL == 4 ? 2 : RL == 2 ? 1 : 0;
   static constexpr int MSK = POW2 ? (RL < 16 ? RL - 1 : 15) : 0;
-  // Lane stride: a multiple of 16 words plus 4.
-  static constexpr int LS = ((M + 15) / 16) * 16 + 4;
+  // Lane stride: a multiple of 16 words plus 16 / min(LANES, 16).  A
+  // half-warp's 16 accesses (64-bit words; 16 words per 128-byte wavefront)
+  // cover 16 / LANES positions of each of LANES lanes, so the lanes must fall
+  // on distinct word residues mod 16: +4 for four lanes, +8 for two, +2 for
+  // eight, an odd stride for 16 or more (a model of the access pattern of the
+  // three rounds puts each of these at one wavefront per half-warp where the
+  // old +4 for every lane count took two to four).
+  static constexpr int LS = ((M + 15) / 16) * 16 + 16 / (LANES < 16 ? LANES : 16);
   static __device__ __forceinline__ int word(int c, int p) {
     return c * LS + (POW2 ? (p ^ ((p >> SH) & MSK)) : p);
   }
@@ -35,8 +41,8 @@ struct gl_p3_layout {
 
 template <int R1, int R2, int R3, int LANES>
 constexpr size_t gl_p3_smem_bytes() {
-  return gl_p3_layout<R1, R2, R3>::NR == 1 ? 0
-                                            : (size_t)LANES * gl_p3_layout<R1, R2, R3>::LS * 8;
+  return gl_p3_layout<R1, R2, R3, LANES>::NR == 1 ? 0
+                                                   : (size_t)LANES * gl_p3_layout<R1, R2, R3, LANES>::LS * 8;
 }
 
 // One CTA's work: tile (bx, by, bz) of the pass described by `a`, with NT
@@ -45,7 +51,7 @@ constexpr size_t gl_p3_smem_bytes() {
 template <int R1, int R2, int R3, int LANES, int NT, bool INV>
 __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int64_t by,
                                           int64_t bz, uint64_t *sm) {
-  using L = gl_p3_layout<R1, R2, R3>;
+  using L = gl_p3_layout<R1, R2, R3, LANES>;
   constexpr int M = L::M;
   constexpr int S1 = R2 * R3;
 
