@@ -118,6 +118,7 @@ int emu_pass3(EMU_ARGS) {
   SHAPE(8, 8, 8, 256)
   SHAPE(16, 8, 8, 512)
   SHAPE(16, 16, 8, 1024)
+  SHAPE(16, 16, 6, 1024)
   return -1;
 }
 
