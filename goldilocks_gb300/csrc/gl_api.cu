@@ -619,7 +619,7 @@ extern "C" int gl_plan_describe(const gl_plan *plan, char *buf, size_t cap) {
   std::string s = plan->tree + " | gpu: ";
   auto kname = [](const gl_kernel_entry *k) {
     std::string t = kernel_shape(k);
-    t.insert(t.size() - 1, ", " + std::to_string(k->lanes) + " lanes");
+    t.insert(t.size() - 1, ", " + std::to_string(k->lanes) + " lanes" + (k->generic ? ", run-time radices" : ""));
     return t;
   };
   if (plan->kind == 0) s += "no-op";

@@ -43,6 +43,19 @@ def test_large_mixed_radix_sizes(gl, oracle, cuda, n):
     assert np.array_equal(from_dev(d), x)
 
 
+@pytest.mark.parametrize("n", [1536 << 11, 2560 << 11, 3072 << 12, 3840 << 12, 1280 << 10, 1920 << 11,
+                               2176 << 11, 2040 << 11])
+def test_compiled_mixed_radix_pass_shapes(gl, oracle, cuda, n):
+    """Lengths whose default split has a 16x16x{6,10,12,15,5}, 16x15x8,
+    16x8x17 or 8x15x17 pass, forward and inverse, against the oracle."""
+    x = gl.fill_uniform(n, seed=0xC0DE, offset=n)
+    d = to_dev(cuda, x)
+    gl.ntt(d)
+    assert np.array_equal(from_dev(d), oracle.ntt(x)), gl.strategy(n).describe()
+    gl.intt(d)
+    assert np.array_equal(from_dev(d), x)
+
+
 @pytest.mark.parametrize("n,count", [(15, 1000), (255, 77), (3840, 9), (12288, 5), (17 << 10, 3)])
 def test_batched_mixed_radix(gl, oracle, cuda, n, count):
     x = rand_field(n * count, seed=n + count)
