@@ -198,6 +198,10 @@ const gl_kernel_entry *gl_find_kernel4(uint64_t m, bool inv) {
   size_t cnt = 0;
   const gl_kernel_entry *e = inv ? gl_kernels_pass_inv(&cnt) : gl_kernels_pass_fwd(&cnt);
   if (const gl_kernel_entry *k = find_in(e, cnt, m)) return k;
+  e = inv ? gl_kernels_mixed35_inv(&cnt) : gl_kernels_mixed35_fwd(&cnt);
+  if (const gl_kernel_entry *k = find_in(e, cnt, m)) return k;
+  e = inv ? gl_kernels_mixed17_inv(&cnt) : gl_kernels_mixed17_fwd(&cnt);
+  if (const gl_kernel_entry *k = find_in(e, cnt, m)) return k;
   return generic_entry(m, inv);  // every other size up to 4096 with radices <= 17
 }
 

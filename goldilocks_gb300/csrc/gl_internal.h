@@ -49,6 +49,11 @@ const gl_kernel_entry *gl_kernels_full_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_full_inv(size_t *count);
 const gl_kernel_entry *gl_kernels_pass_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_pass_inv(size_t *count);
+// Four-lane passes of mixed-radix sizes (factors 3 or 5; factor 17).
+const gl_kernel_entry *gl_kernels_mixed35_fwd(size_t *count);
+const gl_kernel_entry *gl_kernels_mixed35_inv(size_t *count);
+const gl_kernel_entry *gl_kernels_mixed17_fwd(size_t *count);
+const gl_kernel_entry *gl_kernels_mixed17_inv(size_t *count);
 // Passes up to 2048 points with two lanes per CTA and four CTAs per SM.
 const gl_kernel_entry *gl_kernels_pass2_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_pass2_inv(size_t *count);

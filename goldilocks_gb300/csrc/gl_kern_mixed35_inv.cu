@@ -1,0 +1,18 @@
+// Four-lane pass kernels for the pass sizes with a factor 3 or 5 that the default splits of the
+// lengths 3, 5, 15 x 2^k reach, compiled instead of the run-time-radix kernel
+// (inverse).  A unit of its own so that the pass kernels compile in parallel.
+#include "gl_kernels_impl.cuh"
+
+static const gl_kernel_entry k_entries[] = {
+    GL_ENTRY3(16, 16, 6, 4, 1024, true),
+    GL_ENTRY3(16, 16, 10, 4, 1024, true),
+    GL_ENTRY3(16, 16, 12, 4, 1024, true),
+    GL_ENTRY3(16, 16, 15, 4, 1024, true),
+    GL_ENTRY3(16, 16, 5, 4, 1024, true),
+    GL_ENTRY3(16, 15, 8, 4, 1024, true),
+};
+
+const gl_kernel_entry *gl_kernels_mixed35_inv(size_t *count) {
+  *count = sizeof(k_entries) / sizeof(k_entries[0]);
+  return k_entries;
+}

@@ -5,14 +5,7 @@ static const gl_kernel_entry k_entries[] = {
     GL_ENTRY3(8, 8, 1, 4, 32, true),       GL_ENTRY3(16, 8, 1, 4, 32, true),
     GL_ENTRY3(16, 16, 1, 4, 64, true),     GL_ENTRY3(8, 8, 8, 4, 256, true),
     GL_ENTRY3(16, 8, 8, 4, 512, true),     GL_ENTRY3(16, 16, 8, 4, 1024, true),
-    GL_ENTRY3(16, 16, 16, 4, 1024, true),  GL_ENTRY3(16, 15, 17, 4, 1024, true),
-    // Pass sizes with a factor 3, 5 or 17 that the default splits of the
-    // lengths 3, 5, 15, 17, 255 x 2^k reach, compiled instead of the
-    // run-time-radix kernel.
-    GL_ENTRY3(16, 16, 6, 4, 1024, true),   GL_ENTRY3(16, 16, 10, 4, 1024, true),
-    GL_ENTRY3(16, 16, 12, 4, 1024, true),  GL_ENTRY3(16, 16, 15, 4, 1024, true),
-    GL_ENTRY3(16, 16, 5, 4, 1024, true),   GL_ENTRY3(16, 15, 8, 4, 1024, true),
-    GL_ENTRY3(16, 8, 17, 4, 1024, true),   GL_ENTRY3(8, 15, 17, 4, 1024, true),
+    GL_ENTRY3(16, 16, 16, 4, 1024, true),
 };
 
 const gl_kernel_entry *gl_kernels_pass_inv(size_t *count) {
