@@ -228,6 +228,18 @@ static bool pass_size_ok(uint64_t m) { return gl_find_kernel(m, false, false) !=
 
 static bool split_ok(uint64_t m) { return m >= GL_PASS_LANES && m % GL_PASS_LANES == 0 && pass_size_ok(m); }
 
+// Passes of a split that would run on the run-time-radix kernel.
+static int run_time_passes(const gl_choice &c) {
+  const uint64_t f[3] = {c.n1, c.n2, c.n3};
+  int g = 0;
+  for (int s = 0; s < 3; s++)
+    if (f[s]) {
+      const gl_kernel_entry *k = gl_find_kernel(f[s], false, false);
+      g += k && k->generic;
+    }
+  return g;
+}
+
 gl_choice gl_choice_default(uint64_t n) {
   gl_choice c;
   if (n <= 1) { c.kind = 0; return c; }
@@ -249,27 +261,35 @@ gl_choice gl_choice_default(uint64_t n) {
     c.n2 = n / best1;
     return c;
   }
-  // Three passes for n beyond 4096^2: n = n1*n2*n3, all with pass kernels,
-  // the largest factor as small as possible.
-  uint64_t b1 = 0, b2 = 0;
+  // Three passes for n beyond 4096^2: n = n1*n2*n3, all with pass kernels.
+  // Ranked by, in order: fewest passes on the run-time-radix kernel; a first
+  // (column) pass nearest 512 points; a middle pass nearest 64 points; the
+  // largest last (row) pass.  Measured with gl_plan_autotune on GB300, the
+  // fastest splits of 2^25..2^28, 3, 5, 15, 17 and 255 x 2^k were of this
+  // form (512 x 64 x 1024 for 2^25, 512 x 64 x 1088 for 17 x 2^21), 1.1 to
+  // 1.8 times faster than the split with the smallest largest factor.
+  auto dist = [](uint64_t m, int target_log2) {
+    const int l = 63 - __builtin_clzll(m);
+    return l > target_log2 ? l - target_log2 : target_log2 - l;
+  };
+  bool found = false;
+  int best_key[4] = {0, 0, 0, 0};
   for (uint64_t n1 : divisor_list()) {
     if (n1 > 4096) break;
     if (n % n1 || !split_ok(n1)) continue;
     const uint64_t r = n / n1;
     for (uint64_t n2 : divisor_list()) {
       if (n2 > 4096) break;
-      if (r % n2 || !split_ok(n2) || !split_ok(r / n2)) continue;
-      const uint64_t n3 = r / n2;
-      const uint64_t worst = std::max(n1, std::max(n2, n3));
-      if (b1 == 0 || worst < std::max(b1, std::max(b2, n / (b1 * b2))))
-        { b1 = n1; b2 = n2; }
+      if (r % n2 || r / n2 > 4096 || !split_ok(n2) || !split_ok(r / n2)) continue;
+      gl_choice t;
+      t.kind = 3; t.n1 = n1; t.n2 = n2; t.n3 = r / n2;
+      const int key[4] = {run_time_passes(t), dist(n1, 9), dist(n2, 6), -(int)(63 - __builtin_clzll(t.n3))};
+      if (!found || std::lexicographical_compare(key, key + 4, best_key, best_key + 4)) {
+        found = true;
+        std::copy(key, key + 4, best_key);
+        c = t;
+      }
     }
-  }
-  if (b1) {
-    c.kind = 3;
-    c.n1 = b1;
-    c.n2 = b2;
-    c.n3 = n / (b1 * b2);
   }
   return c;  // kind -1: a divisor without a GPU schedule
 }
@@ -318,10 +338,22 @@ std::vector<gl_choice> gl_choice_candidates(uint64_t n) {
     }
   }
   auto worst = [](const gl_choice &c) { return std::max(c.n1, std::max(c.n2, c.n3)); };
-  std::stable_sort(tri.begin(), tri.end(),
+  auto by_worst = tri;
+  std::stable_sort(by_worst.begin(), by_worst.end(),
                    [&](const gl_choice &a, const gl_choice &b) { return worst(a) < worst(b); });
-  if (tri.size() > 6) tri.resize(6);
-  for (const gl_choice &c : tri) add(c);
+  if (by_worst.size() > 6) by_worst.resize(6);
+  for (const gl_choice &c : by_worst) add(c);
+  // And the splits with the fewest passes on the run-time-radix kernel, the
+  // ones starting with a 512-point pass first.
+  auto by_compiled = tri;
+  std::stable_sort(by_compiled.begin(), by_compiled.end(), [&](const gl_choice &a, const gl_choice &b) {
+    const int ga = run_time_passes(a), gb = run_time_passes(b);
+    if (ga != gb) return ga < gb;
+    if ((a.n1 == 512) != (b.n1 == 512)) return a.n1 == 512;
+    return worst(a) < worst(b);
+  });
+  if (by_compiled.size() > 6) by_compiled.resize(6);
+  for (const gl_choice &c : by_compiled) add(c);
   return out;
 }
 
