@@ -244,7 +244,25 @@ gl_choice gl_choice_default(uint64_t n) {
   gl_choice c;
   if (n <= 1) { c.kind = 0; return c; }
   if (gl_find_kernel(n, true, false)) { c.kind = 1; return c; }
-  // Four-step: prefer n1 <= n2 nearest sqrt(n), both with pass kernels.
+  // Four-step with a short first (column) pass and four-lane kernels: 512
+  // points when the rest is 128..4096 points (2^16..2^21 and the mixed
+  // lengths near 2^20), else 64 points up to 2^15.  Measured with
+  // gl_plan_autotune on GB300 these were the fastest splits of those lengths,
+  // 1.14-1.33 times faster than the split nearest sqrt(n) (2^17 and 2^18
+  // are 512 x n/512 either way).
+  for (const uint64_t n1 : {512ull, 64ull}) {
+    const uint64_t n2 = n / n1;
+    if (n % n1 || !split_ok(n1) || !split_ok(n2)) continue;
+    if (n1 == 512 && (n2 < 128 || n2 > 4096)) continue;
+    if (n1 == 64 && n > (1ull << 15)) continue;
+    if (gl_find_kernel(n2, false, false)->generic) continue;  // measured with compiled passes only
+    c.kind = 2;
+    c.n1 = n1;
+    c.n2 = n2;
+    c.lanes4 = 1;
+    return c;
+  }
+  // Otherwise: n1 <= n2 nearest sqrt(n), both with pass kernels.
   uint64_t best1 = 0;
   for (uint64_t n1 : divisor_list()) {
     if (n1 > n) break;

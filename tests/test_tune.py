@@ -23,13 +23,13 @@ def tuned(gl):
 
 def test_load_applies_schedule(gl, tuned, tmp_path):
     before = _gpu_part(gl.strategy(1 << 20).describe())
-    assert before.startswith("col 1024")
+    assert before.startswith("col 512") and "4 lanes" in before, before
     f = tmp_path / "t.json"
     f.write_text(json.dumps({"format": "goldilocks-gb300-tuning", "version": 1, "device": "x",
-                             "plans": [{"size": 1 << 20, "kind": 2, "factors": [512, 2048], "lanes": 4}]}))
+                             "plans": [{"size": 1 << 20, "kind": 2, "factors": [1024, 1024], "lanes": 2}]}))
     tuned.load(str(f))
     after = _gpu_part(gl.strategy(1 << 20).describe())
-    assert after.startswith("col 512") and "row 2048" in after and "4 lanes" in after, after
+    assert after.startswith("col 1024") and "row 1024" in after and "2 lanes" in after, after
     # The schedule survives clear_cache: it is a tuned choice, not a cached plan.
     gl.clear_cache()
     assert _gpu_part(gl.strategy(1 << 20).describe()) == after
@@ -148,7 +148,7 @@ def test_tuning_file_from_environment(gl, tmp_path):
     import sys
     f = tmp_path / "env.json"
     f.write_text(json.dumps({"format": "goldilocks-gb300-tuning", "version": 1,
-                             "plans": [{"size": 1 << 20, "kind": 2, "factors": [512, 2048], "lanes": 4}]}))
+                             "plans": [{"size": 1 << 20, "kind": 2, "factors": [1024, 1024], "lanes": 2}]}))
     code = ("import goldilocks_gb300 as G; "
             "print(G.strategy(1 << 20).describe().split(' | gpu: ')[1])")
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -156,11 +156,11 @@ def test_tuning_file_from_environment(gl, tmp_path):
     out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
                          timeout=120, cwd=root)
     assert out.returncode == 0, out.stderr
-    assert out.stdout.startswith("col 512") and "4 lanes" in out.stdout, out.stdout
+    assert out.stdout.startswith("col 1024") and "2 lanes" in out.stdout, out.stdout
     env["GOLDILOCKS_TUNING"] = str(tmp_path / "missing.json")
     out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
                          timeout=120, cwd=root)
-    assert out.returncode == 0 and out.stdout.startswith("col 1024"), out.stdout + out.stderr
+    assert out.returncode == 0 and out.stdout.startswith("col 512"), out.stdout + out.stderr
     assert "not loaded" in out.stderr
 
 
@@ -183,7 +183,7 @@ def test_bucket_batches_after_a_schedule_change(gl, cuda, oracle, tuned, tmp_pat
     run()
     run()  # replayed from the graph
     f = tmp_path / "t.json"
-    for plan in ({"size": n, "kind": 2, "factors": [64, 256], "lanes": 4},
+    for plan in ({"size": n, "kind": 2, "factors": [128, 128], "lanes": 4},
                  {"size": n, "kind": 3, "factors": [16, 32, 32]}):
         f.write_text(json.dumps({"format": "goldilocks-gb300-tuning", "version": 1, "plans": [plan]}))
         tuned.load(str(f))
@@ -198,13 +198,13 @@ def test_explicit_calls_take_precedence_over_the_environment_file(gl, tmp_path):
     import subprocess
     import sys
     env_file, own = tmp_path / "env.json", tmp_path / "own.json"
-    for path, split in ((env_file, [256, 4096]), (own, [512, 2048])):
+    for path, split in ((env_file, [256, 4096]), (own, [1024, 1024])):
         path.write_text(json.dumps({"format": "goldilocks-gb300-tuning", "version": 1,
                                     "plans": [{"size": 1 << 20, "kind": 2, "factors": split}]}))
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     env = dict(os.environ, GOLDILOCKS_TUNING=str(env_file), PYTHONPATH=root)
     show = "print(G.strategy(1 << 20).describe().split(' | gpu: ')[1])"
-    for code, want in (("T.load(%r)" % str(own), "col 512"), ("T.clear()", "col 1024"), ("pass", "col 256")):
+    for code, want in (("T.load(%r)" % str(own), "col 1024"), ("T.clear()", "col 512"), ("pass", "col 256")):
         prog = "import goldilocks_gb300 as G; from goldilocks_gb300 import tune as T; %s; %s" % (code, show)
         out = subprocess.run([sys.executable, "-c", prog], env=env, capture_output=True, text=True,
                              timeout=120, cwd=root)
