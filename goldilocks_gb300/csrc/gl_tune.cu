@@ -6,7 +6,8 @@
 //
 //   gl_plan_autotune(size)  times every candidate schedule of `size` (the
 //                           default, every two-pass split, the six three-pass
-//                           splits with the smallest largest factor, each
+//                           splits with the smallest largest factor and the
+//                           six with the fewest run-time-radix passes, each
 //                           with two- and four-lane pass kernels), checks
 //                           that each one's output equals the default's word
 //                           for word, and makes the fastest the plan of that
