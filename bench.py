@@ -218,6 +218,21 @@ def bench_batched(gl, torch, reps=3):
         b.synchronize()
         out[name + "_elem_s"] = out["elements"] * reps / (a.elapsed_time(b) * 1e-3)
     out["persistent_vs_per_call"] = out["persistent_elem_s"] / out["per_call_elem_s"]
+    # The same batch through run_packed: (offset, length, direction) arrays
+    # over the pool, so the host builds the descriptor array in one numpy
+    # step instead of one Python call per polynomial.
+    offs = np.cumsum([0] + sizes[:-1])
+    dirs = [i % 2 for i in range(len(sizes))]
+    for name, mode in (("buckets_packed", B.BUCKETS), ("persistent_packed", B.PERSISTENT)):
+        B.run_packed(pool, offs, sizes, dirs, mode=mode)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            B.run_packed(pool, offs, sizes, dirs, mode=mode)
+        b.record(stream)
+        b.synchronize()
+        out[name + "_elem_s"] = out["elements"] * reps / (a.elapsed_time(b) * 1e-3)
     # The schedules of the batch's lengths measured first (gl_plan_autotune),
     # then buckets again, and AUTO with the mode gl_batch_autotune measured.
     from goldilocks_gb300 import tune

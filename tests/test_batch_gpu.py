@@ -122,3 +122,40 @@ def test_batch_with_three_pass_and_rader_lengths(gl, oracle, cuda, mode_name):
     B.run(list(zip(ds, dirs)), mode=mode)
     for x, d, inv in zip(xs, ds, dirs):
         assert np.array_equal(from_dev(d), (oracle.intt if inv else oracle.ntt)(x)), x.size
+
+
+@pytest.mark.parametrize("mode_name", ["PERSISTENT", "BUCKETS", "PER_CALL", "AUTO"])
+def test_packed_batches_match_oracle(gl, oracle, cuda, mode_name):
+    """run_packed over one pool tensor, with gaps between the polynomials that
+    must stay untouched, against the oracle per polynomial."""
+    from goldilocks_gb300 import batch as B
+    sizes = [4096, 8192, 1 << 16, 64, 3 << 12, 1 << 13, 1 << 18, 17 << 10, 16, 1 << 15]
+    gap = 5
+    offs, off = [], 0
+    for n in sizes:
+        offs.append(off)
+        off += n + gap
+    x = rand_field(off, seed=77)
+    pool = to_dev(cuda, x)
+    dirs = [i % 2 for i in range(len(sizes))]
+    B.run_packed(pool, offs, sizes, dirs, mode=getattr(B, mode_name))
+    y = from_dev(pool)
+    for o, n, d in zip(offs, sizes, dirs):
+        src = x[o:o + n]
+        want = oracle.intt(src) if d else oracle.ntt(src)
+        assert np.array_equal(y[o:o + n], want), (n, d)
+        assert np.array_equal(y[o + n:o + n + gap], x[o + n:o + n + gap]), n
+
+
+def test_packed_batch_argument_checks(gl, cuda):
+    from goldilocks_gb300 import batch as B
+    pool = cuda.zeros(100, dtype=cuda.int64, device="cuda")
+    with pytest.raises(ValueError):
+        B.run_packed(pool, [0, 64], [64, 64], [0, 1])          # past the end of the pool
+    with pytest.raises(ValueError):
+        B.run_packed(pool, [0], [64, 32], [0])                 # ragged arrays
+    with pytest.raises(ValueError):
+        B.run_packed(pool[::2], [0], [32], [0])                # not contiguous
+    with pytest.raises(ValueError, match="not a supported NTT size"):
+        B.run_packed(pool, [0], [7], [0])
+    B.run_packed(pool, [], [], [])                             # empty: nothing to do

@@ -41,3 +41,4 @@ def test_ring_rejects_oversized_outputs():
         pass
     else:
         raise AssertionError("expected ValueError")
+
