@@ -33,6 +33,8 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, default=0,
                     help="time batches of this many polynomials, log2 n uniform in [12, 18] (seeded)")
     ap.add_argument("--batch-mode", choices=["auto", "persistent", "buckets", "per_call"], default="auto")
+    ap.add_argument("--batch-api", choices=["packed", "list"], default="packed",
+                    help="batch.run_packed (offsets into one pool) or batch.run (a list of tensors)")
     ap.add_argument("--tune", type=str, default="",
                     help="autotune each size's schedule first and save the choices to this JSON file")
     args = ap.parse_args(argv)
@@ -123,19 +125,27 @@ def _run_batch(args, gl, torch, np):
         off += n
     mode = {"auto": B.AUTO, "persistent": B.PERSISTENT, "buckets": B.BUCKETS, "per_call": B.PER_CALL}[args.batch_mode]
     stream = torch.cuda.current_stream()
+    offs = np.cumsum([0] + sizes[:-1])
+    dirs = [i % 2 for i in range(len(sizes))]
+
+    def run():
+        if args.batch_api == "packed":
+            B.run_packed(pool, offs, sizes, dirs, mode=mode)
+        else:
+            B.run(items, mode=mode)
     for _ in range(args.warmup):
-        B.run(items, mode=mode)
+        run()
     times = []
     for _ in range(args.reps):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        B.run(items, mode=mode)
+        run()
         b.record(stream)
         b.synchronize()
         times.append(a.elapsed_time(b) * 1e-3)
     t = statistics.median(times)
-    print("polys,mode,elements,duration,throughput")
-    print("%d,%s,%d,%.9f,%.6e" % (len(sizes), args.batch_mode, sum(sizes), t, sum(sizes) / t))
+    print("polys,mode,api,elements,duration,throughput")
+    print("%d,%s,%s,%d,%.9f,%.6e" % (len(sizes), args.batch_mode, args.batch_api, sum(sizes), t, sum(sizes) / t))
     return 0
 
 
