@@ -280,9 +280,9 @@ gl_choice gl_choice_default(uint64_t n) {
     return c;
   }
   // Three passes for n beyond 4096^2: n = n1*n2*n3, all with pass kernels.
-  // Ranked by, in order: fewest passes on the run-time-radix kernel; a first
-  // (column) pass nearest 512 points; a middle pass nearest 64 points; the
-  // largest last (row) pass.  Measured with gl_plan_autotune on GB300, the
+  // Ranked by, in order: fewest passes on the run-time-radix kernel; a
+  // power-of-two first (column) pass, nearest 512 points; a middle pass
+  // nearest 64 points; the largest last (row) pass.  Measured with gl_plan_autotune on GB300, the
   // fastest splits of 2^25..2^28, 3, 5, 15, 17 and 255 x 2^k were of this
   // form (512 x 64 x 1024 for 2^25, 512 x 64 x 1088 for 17 x 2^21), 1.1 to
   // 1.8 times faster than the split with the smallest largest factor.
@@ -291,7 +291,7 @@ gl_choice gl_choice_default(uint64_t n) {
     return l > target_log2 ? l - target_log2 : target_log2 - l;
   };
   bool found = false;
-  int best_key[4] = {0, 0, 0, 0};
+  int best_key[5] = {0, 0, 0, 0, 0};
   for (uint64_t n1 : divisor_list()) {
     if (n1 > 4096) break;
     if (n % n1 || !split_ok(n1)) continue;
@@ -301,10 +301,11 @@ gl_choice gl_choice_default(uint64_t n) {
       if (r % n2 || r / n2 > 4096 || !split_ok(n2) || !split_ok(r / n2)) continue;
       gl_choice t;
       t.kind = 3; t.n1 = n1; t.n2 = n2; t.n3 = r / n2;
-      const int key[4] = {run_time_passes(t), dist(n1, 9), dist(n2, 6), -(int)(63 - __builtin_clzll(t.n3))};
-      if (!found || std::lexicographical_compare(key, key + 4, best_key, best_key + 4)) {
+      const int key[5] = {run_time_passes(t), (n1 & (n1 - 1)) != 0, dist(n1, 9), dist(n2, 6),
+                          -(int)(63 - __builtin_clzll(t.n3))};
+      if (!found || std::lexicographical_compare(key, key + 5, best_key, best_key + 5)) {
         found = true;
-        std::copy(key, key + 4, best_key);
+        std::copy(key, key + 5, best_key);
         c = t;
       }
     }

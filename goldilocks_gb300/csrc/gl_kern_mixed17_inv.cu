@@ -13,6 +13,12 @@ static const gl_kernel_entry k_entries[] = {
     GL_ENTRY3M(16, 5, 17, 4, 512, 2, true),
     GL_ENTRY3M(16, 6, 17, 4, 512, 2, true),
     GL_ENTRY3M(16, 4, 17, 4, 512, 2, true),
+    // 272..680 points (lengths up to about 2^19).
+    GL_ENTRY3(16, 17, 1, 4, 64, true),
+    GL_ENTRY3(16, 17, 2, 4, 256, true),
+    GL_ENTRY3(8, 5, 17, 4, 256, true),
+    GL_ENTRY3(8, 3, 17, 4, 256, true),
+    GL_ENTRY3(17, 10, 2, 4, 256, true),
 };
 
 const gl_kernel_entry *gl_kernels_mixed17_inv(size_t *count) {

@@ -10,6 +10,12 @@ static const gl_kernel_entry k_entries[] = {
     GL_ENTRY3(16, 16, 15, 4, 1024, true),
     GL_ENTRY3(16, 16, 5, 4, 1024, true),
     GL_ENTRY3(16, 15, 8, 4, 1024, true),
+    // 320..768 points (lengths up to about 2^19): 256 threads.
+    GL_ENTRY3(16, 16, 3, 4, 256, true),
+    GL_ENTRY3(16, 10, 4, 4, 256, true),
+    GL_ENTRY3(16, 15, 2, 4, 256, true),
+    GL_ENTRY3(16, 8, 3, 4, 256, true),
+    GL_ENTRY3(16, 10, 2, 4, 256, true),
 };
 
 const gl_kernel_entry *gl_kernels_mixed35_inv(size_t *count) {

@@ -63,7 +63,8 @@ def test_no_compiled_shape_left_unused(gl):
     kernel uses it: the run-time-radix kernel only appears for pass sizes that
     have none (the two are labelled apart)."""
     compiled = {"1536", "2560", "3072", "3840", "1280", "1920", "4080", "2176", "2040",
-                "2720", "3264", "1360", "1632", "1088"}
+                "2720", "3264", "1360", "1632", "1088", "768", "640", "480", "384", "320",
+                "272", "544", "680", "408", "340"}
     for n in gl.divisors():
         if n <= 4096 or n > 1 << 24 or n % 257 == 0 or n % 65537 == 0:
             continue
@@ -71,3 +72,10 @@ def test_no_compiled_shape_left_unused(gl):
             size = part.split()[1]
             if size in compiled:
                 assert "run-time radices" not in part, (n, part)
+
+
+def test_no_run_time_radix_pass_from_2p16_to_2p24(gl):
+    for n in gl.divisors():
+        if n < 1 << 16 or n > 1 << 24 or n % 257 == 0 or n % 65537 == 0:
+            continue
+        assert "run-time radices" not in gpu(gl, n), (n, gpu(gl, n))

@@ -45,11 +45,12 @@ def test_large_mixed_radix_sizes(gl, oracle, cuda, n):
 
 @pytest.mark.parametrize("n", [1536 << 11, 2560 << 11, 3072 << 12, 3840 << 12, 1280 << 10, 1920 << 11,
                                2176 << 11, 2040 << 11, 1088 << 10, 1360 << 11, 1632 << 11, 2720 << 12,
-                               3264 << 12])
+                               3264 << 12, 393216, 327680, 245760, 196608, 278528, 522240, 208896,
+                               174080, 417792, 491520])
 def test_compiled_mixed_radix_pass_shapes(gl, oracle, cuda, n):
-    """Lengths whose default split has a compiled mixed-radix pass
-    (16x16x{5,6,10,12,15}, 16x15x8, 16x{4,5,6,8,10,12}x17, 8x15x17), forward
-    and inverse, against the oracle."""
+    """Lengths whose default split has a compiled mixed-radix pass (the
+    gl_kern_mixed35 and gl_kern_mixed17 shapes), forward and inverse, against
+    the oracle."""
     x = gl.fill_uniform(n, seed=0xC0DE, offset=n)
     d = to_dev(cuda, x)
     gl.ntt(d)
