@@ -119,6 +119,9 @@ int emu_pass3(EMU_ARGS) {
   SHAPE(16, 8, 8, 512)
   SHAPE(16, 16, 8, 1024)
   SHAPE(16, 16, 6, 1024)
+  SHAPE(16, 17, 1, 64)
+  SHAPE(8, 5, 17, 256)
+  SHAPE(16, 10, 2, 256)
   return -1;
 }
 

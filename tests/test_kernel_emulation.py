@@ -74,6 +74,7 @@ def call(emu, shape, inv, x, out, in_ls, in_is, out_ls, out_is, lanes, flags, tw
 
 
 @pytest.mark.parametrize("shape", [(8, 8, 1), (16, 16, 1), (8, 8, 8), (16, 8, 8), (16, 16, 6),
+                                   (16, 17, 1), (8, 5, 17), (16, 10, 2),
                                    ("gen", 3, 1, 1), ("gen", 17, 1, 1), ("gen", 17, 15, 1),
                                    ("gen", 12, 10, 1), ("gen", 5, 6, 17), ("gen", 17, 16, 15)])
 @pytest.mark.parametrize("inv", [False, True])
