@@ -1266,7 +1266,7 @@ extern "C" int gl_ntt_columns(uint64_t *data, uint64_t rows, uint64_t cols, int 
                               void *stream_) {
   GL_NVTX("gl_ntt_columns");
   cudaStream_t stream = (cudaStream_t)stream_;
-  if ((!data && rows * cols) || (dir != GL_FORWARD && dir != GL_INVERSE) ||
+  if ((!data && rows != 0 && cols != 0) || (dir != GL_FORWARD && dir != GL_INVERSE) ||
       (mem != GL_MEM_HOST && mem != GL_MEM_DEVICE))
     return GL_ERR_INVALID;
   if (rows == 0 || cols == 0) return rows == 0 ? GL_ERR_UNSUPPORTED_SIZE : GL_OK;
