@@ -210,3 +210,36 @@ def test_explicit_calls_take_precedence_over_the_environment_file(gl, tmp_path):
                              timeout=120, cwd=root)
         assert out.returncode == 0, out.stderr
         assert out.stdout.startswith(want), (code, out.stdout)
+
+
+@pytest.mark.parametrize("doc,ok", [
+    # unknown keys, string escapes, whitespace and an omitted "lanes" are accepted
+    ('{"format": "goldilocks-gb300-tuning", "version": 1, "device": "GB\\u0033\\u0030\\u0030 \\"x\\"\\n",'
+     ' "extra": [1, 2.5e3, true, false, null, {"a": {}}], "plans": [ {"size" : 1048576 , "kind": 2,'
+     ' "factors": [1024, 1024], "note": "x"} ] }', True),
+    ('{"format": "goldilocks-gb300-tuning", "version": 1, "plans": [], "batches": []}', True),
+    # numbers that are not plain non-negative integers
+    ('{"format": "goldilocks-gb300-tuning", "version": 1, "plans": [{"size": 1.048576e6, "kind": 2,'
+     ' "factors": [1024, 1024]}]}', False),
+    ('{"format": "goldilocks-gb300-tuning", "version": 1, "plans": [{"size": -1048576, "kind": 2,'
+     ' "factors": [1024, 1024]}]}', False),
+    ('{"format": "goldilocks-gb300-tuning", "version": 1, "plans": [{"size": 18446744073709551616,'
+     ' "kind": 2, "factors": [1024, 1024]}]}', False),
+    # malformed JSON
+    ('{"format": "goldilocks-gb300-tuning", "version": 1, "plans": [{"size": 1048576,}]}', False),
+    ('{"format": "goldilocks-gb300-tuning" "version": 1}', False),
+    ('{"format": "goldilocks-gb300-tuning", "version": 01}', False),
+    ('{"format": "goldilocks-gb300-tuning\\x", "version": 1}', False),
+    ('', False),
+])
+def test_tuning_file_grammar(gl, tuned, tmp_path, doc, ok):
+    from goldilocks_gb300 import _lib as L
+    from goldilocks_gb300.ntt import GoldilocksError
+    f = tmp_path / "g.json"
+    f.write_text(doc)
+    if ok:
+        tuned.load(str(f))
+    else:
+        with pytest.raises(GoldilocksError) as e:
+            tuned.load(str(f))
+        assert e.value.status == L.GL_ERR_INVALID
