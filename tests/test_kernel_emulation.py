@@ -115,6 +115,39 @@ def four_step(emu, n1, n2, shape1, shape2, x, inv=False, C=1, in_limit=NOLIM, co
     return out
 
 
+def three_step(emu, n1, n2, n3, shapes, x, inv=False):
+    """COL(n1) to scratch, COL(n2) in place per k1, ROW(n3) back, exactly as the
+    library schedules a three-pass plan of one contiguous sequence (C = 1):
+    j = n2 n3 j1 + n3 j2 + j3, k = k1 + n1 k2 + n1 n2 k3."""
+    n, n23 = n1 * n2 * n3, n2 * n3
+    s1 = np.zeros(n, dtype=np.uint64)
+    out = np.zeros(n, dtype=np.uint64)
+    w = root(n, inv)
+    scale = pow(n, P - 2, P) if inv else 1
+    lo, hi = table(w, 4096, scale), table(pow(w, 4096, P), (n + 4095) // 4096)
+    w23 = root(n23, inv)
+    lo23, hi23 = table(w23, 4096), table(pow(w23, 4096, P), (n23 + 4095) // 4096)
+    t1, t2, t3 = table(root(n1, inv), n1), table(root(n2, inv), n2), table(root(n3, inv), n3)
+    flags = F_PASS_TW | F_LOAD_LF | F_STORE_LF
+    call(emu, shapes[0], inv, x, s1, 1, n23, 1, n23, n23, flags | F_CANON_IN, t1, t1, lo, hi)
+    for k1 in range(n1):  # grid.y of the middle pass: one n23 block per k1, in place
+        blk = s1[k1 * n23:(k1 + 1) * n23]
+        call(emu, shapes[1], inv, blk, blk, 1, n3, 1, n3, n3, flags, t2, t2, lo23, hi23)
+    for k1 in range(n1):  # grid.y of the last pass: rows k2 of block k1, stored at k1 + n1 k
+        call(emu, shapes[2], inv, s1[k1 * n23:(k1 + 1) * n23], out[k1:], n3, 1, n1, n1 * n2, n2,
+             F_STORE_LF, t3, t3)
+    return out
+
+
+@pytest.mark.parametrize("inv", [False, True])
+def test_three_step(emu, oracle, inv):
+    """The three-pass schedule's index and twiddle arithmetic: 64 x 64 x 256."""
+    n1, n2, n3 = 64, 64, 256
+    x = rand_field(n1 * n2 * n3, seed=23 + inv)
+    got = three_step(emu, n1, n2, n3, [(8, 8, 1), (8, 8, 1), (16, 16, 1)], x, inv)
+    assert np.array_equal(got, (oracle.intt if inv else oracle.ntt)(x))
+
+
 @pytest.mark.parametrize("inv", [False, True])
 def test_four_step(emu, oracle, inv):
     n1, n2 = 64, 512
