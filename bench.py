@@ -477,7 +477,7 @@ def run_ours(args):
         h = torch.empty(n, dtype=torch.int64, pin_memory=True)
         h.numpy().view(np.uint64)[:] = gl.fill_uniform(n, seed=0xE2E0 + i)
         hosts.append(h.numpy().view(np.uint64))
-    e2e_steps = max(1, min(args.steps, 5))
+    e2e_steps = max(1, min(args.steps, 20))
 
     def host_step():
         # gl_host_pipeline: each buffer goes to the GPU once, gets the forward
