@@ -48,7 +48,7 @@ WORKLOAD = {"workload": "large single transforms, plain per-call: forward+invers
                         "n=2^20, 2^22, 2^24, 16711680 (2^16*3*5*17)",
             "sizes": SIZES, "transforms_per_step": 2 * len(SIZES),
             "elements_per_step": 2 * sum(SIZES), "field": "Goldilocks p=2^64-2^32+1",
-            "inputs": "uniform in [0,p), seeded (gl_fill_uniform)",
+            "inputs": "uniform in [0,p), seeded splitmix64 stream (gl_fill_uniform; oracle.fill_uniform for the CPU legs)",
             "l2": "flushed between steps (256 MiB write, outside timed events)"}
 
 
@@ -146,21 +146,56 @@ def ncu_traffic():
     return ncu_per_element("ncu_traffic.json")
 
 
-def cpu_oracle_step(threads):
-    """One step of the workload on the CPU oracle; returns (elements, seconds)."""
-    import numpy as np
+def host_cpu():
+    """The host's usable threads and CPU model (x86 'model name', or the Arm
+    implementer/part codes when /proc/cpuinfo has no model name)."""
+    try:
+        usable = len(os.sched_getaffinity(0))
+    except Exception:
+        usable = os.cpu_count() or 1
+    model, arm = None, {}
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k, _, v = line.partition(":")
+                k, v = k.strip(), v.strip()
+                if k == "model name" and model is None:
+                    model = v
+                elif k in ("CPU implementer", "CPU part") and k not in arm:
+                    arm[k] = v
+    except OSError:
+        pass
+    if model is None:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=5).stdout
+            for line in out.splitlines():
+                if line.startswith("Model name:"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except Exception:
+            pass
+    if model is None and arm:
+        model = "arm implementer %s part %s" % (arm.get("CPU implementer"), arm.get("CPU part"))
+    return {"nproc": os.cpu_count(), "usable_threads": usable, "model": model}
 
+
+def cpu_oracle_run(steps, threads):
+    """`steps` steps of the workload on the CPU oracle, every transform of
+    every step one job on a pool of `threads` host threads (a transform runs
+    on one thread, as the reference's does below its parallel work size
+    MIN_WORK_SIZE = 2^24 elements); returns (elements, seconds).  The inputs
+    come from the oracle's own generator (the same seeded stream as the GPU
+    arm's), so this leg never loads the product library."""
     import oracle
     oracle.build()
-    from goldilocks_gb300 import fill_uniform
-    inputs = [fill_uniform(n, seed=0xC0 + i) for i, n in enumerate(SIZES)]
+    inputs = [oracle.fill_uniform(n, seed=0xC0 + i) for i, n in enumerate(SIZES)]
 
     def job(args):
         i, inv = args
         x = inputs[i]
         return (oracle.intt(x) if inv else oracle.ntt(x)).size
 
-    jobs = [(i, inv) for i in range(len(SIZES)) for inv in (0, 1)]
+    jobs = [(i, inv) for _ in range(steps) for i in range(len(SIZES)) for inv in (0, 1)]
     t0 = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as ex:
         total = sum(ex.map(job, jobs))
@@ -171,23 +206,21 @@ def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
         return 0
-    threads = min(len(SIZES) * 2, os.cpu_count() or 1)
-    for _ in range(args.warmup):
-        cpu_oracle_step(threads)
-    tot_el, tot_s = 0, 0.0
-    for _ in range(args.steps):
-        el, s = cpu_oracle_step(threads)
-        tot_el += el
-        tot_s += s
+    cpu = host_cpu()
+    threads = cpu["usable_threads"]
+    if args.warmup > 0:
+        cpu_oracle_run(1, threads)
+    tot_el, tot_s = cpu_oracle_run(args.steps, threads)
     v = tot_el / tot_s
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (mod p)",
             "data": "synthetic", "config": WORKLOAD,
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "the full step: 8 transforms, one per host thread; C restatement "
-                                       "of the reference CPU algorithm (no Rust toolchain to build the "
-                                       "reference itself)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "host": cpu,
+                             "sample": "%d steps of 8 transforms on a pool of %d host threads (one "
+                                       "transform per thread); C restatement of the reference CPU "
+                                       "algorithm (no Rust toolchain to build the reference itself)"
+                                       % (args.steps, threads)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -567,7 +600,7 @@ def run_ours(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64 (mod p)", "data": "synthetic",
-            "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single GPU"),
+            "config": WORKLOAD, "parallelism": "replicas" if world > 1 else "single GPU",
             "roofline": roofline,
             "issue_roofline": issue,
             "step_roofline": {"algorithmic_bytes_per_step": alg_bytes,
@@ -597,11 +630,14 @@ def run_ours(args):
             line["commit"]["cpu_oracle_k12_blocks_per_s_1_thread"] = k12_rate
             line["pow"]["cpu_oracle_hashes_per_s_1_thread"] = k12_rate
     if world == 1 and not args.no_cpu_baseline:
-        threads = min(2 * len(SIZES), os.cpu_count() or 1)
-        el, s = cpu_oracle_step(threads)
+        cpu = host_cpu()
+        threads = cpu["usable_threads"]
+        el, s = cpu_oracle_run(2, threads)
         line["cpu_baseline"] = {"value": el / s, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": "one full step (8 transforms, one per thread) of the C "
-                                          "restatement of the reference CPU algorithm"}
+                                "host": cpu,
+                                "sample": "two steps (16 transforms) of the C restatement of the "
+                                          "reference CPU algorithm on a pool of %d host threads, one "
+                                          "transform per thread" % threads}
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

@@ -4,7 +4,10 @@
 // memory pool or other allocating routine is called on this path.
 //
 // The scratch array and the twiddle-table array below exist on every GPU that
-// loads the library, from load until the process exits (8 MiB + 50 KiB).
+// loads the library's device code, from then until the process exits (8 MiB +
+// 50 KiB).  With CUDA's lazy module loading (the default) that device code is
+// loaded by the first call on each device, which can itself take device
+// memory: make that first call during set-up.
 #include <cuda_runtime.h>
 
 #include <map>
@@ -40,15 +43,17 @@ std::map<int, noalloc_ptrs> g_ptrs;  // per device
 int device_ptrs(noalloc_ptrs *out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return GL_ERR_CUDA;
+  if (e != cudaSuccess) return gl_cuda_status(e);
   std::lock_guard<std::mutex> lk(g_mu);
   auto it = g_ptrs.find(dev);
   if (it == g_ptrs.end()) {
     noalloc_ptrs p{};
+    // Under lazy module loading this is also where the module holding the
+    // arrays and the pass kernels is loaded onto the device.
     e = cudaGetSymbolAddress((void **)&p.scratch, g_noalloc_scratch);
-    if (e != cudaSuccess) return GL_ERR_CUDA;
+    if (e != cudaSuccess) return gl_cuda_status(e);
     e = cudaGetSymbolAddress((void **)&p.tables, g_noalloc_tables);
-    if (e != cudaSuccess) return GL_ERR_CUDA;
+    if (e != cudaSuccess) return gl_cuda_status(e);
     it = g_ptrs.emplace(dev, p).first;
   }
   *out = it->second;
@@ -130,5 +135,5 @@ extern "C" int gl_ntt_noalloc(uint64_t *data, uint64_t len, int dir, void *strea
   b.tw_m = b.tw_r2 = tab + GL_NOALLOC_T2;
   kr->launch(b, dim3((unsigned)gl_tiles(n1, kr)), stream);
 
-  return cudaGetLastError() == cudaSuccess ? GL_OK : GL_ERR_CUDA;
+  return gl_cuda_status(cudaGetLastError());
 }

@@ -344,8 +344,11 @@ int gl_server_destroy(gl_server *srv);
  * Lengths: powers of two from 2^13 to GL_NTT_NOALLOC_MAX_LEN; longer or
  * non-power-of-two lengths return GL_ERR_INVALID (non-divisors of p - 1:
  * GL_ERR_UNSUPPORTED_SIZE).  The first call on each device looks up the
- * device addresses of the fixed arrays (cudaGetSymbolAddress); make that
- * first call before any stream capture.  All calls share the arrays, so calls
+ * device addresses of the fixed arrays (cudaGetSymbolAddress); under CUDA's
+ * lazy module loading (the default) it is also the call that loads the
+ * library's device code onto that device, which takes device memory of its
+ * own.  So make that first call during set-up, while memory is still
+ * available, and before any stream capture.  All calls share the arrays, so calls
  * that overlap on the GPU (different streams without ordering) race: order
  * them on one stream or synchronise between them.  Each call writes every
  * array word it later reads, so nothing needs clearing between calls. */

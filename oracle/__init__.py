@@ -35,7 +35,10 @@ def build():
     for src in SOURCES:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         objs.append(obj)
-        procs.append(subprocess.Popen(["gcc", "-O2", "-fPIC", "-std=c11", "-c", src, "-o", obj],
+        # -O3 without -march=native: the same build recipe runs on the x86
+        # container and on the Arm host of the GPU, and must give the same code
+        # paths on both (the arithmetic is integer-only, so results agree).
+        procs.append(subprocess.Popen(["gcc", "-O3", "-fPIC", "-std=c11", "-c", src, "-o", obj],
                                       stderr=subprocess.PIPE, text=True))
     for p in procs:
         _, err = p.communicate()
@@ -211,6 +214,36 @@ def strategy_describe(size):
     if lib().glo_strategy_describe(size, buf, len(buf)):
         raise ValueError("oracle: unsupported size")
     return buf.value.decode()
+
+
+_M64 = (1 << 64) - 1
+
+
+def _splitmix64(x):
+    """splitmix64 finaliser on a numpy uint64 array (wrapping arithmetic)."""
+    z = x + np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def fill_uniform(n, seed, offset=0):
+    """Seeded field elements uniform in [0, p): element i is the first value
+    below p of splitmix64(splitmix64(seed) ^ (offset + i + (k << 48))),
+    k = 0, 1, ...  The same stream as the GPU library's gl_fill_uniform,
+    restated in numpy so that the CPU baseline makes its inputs without
+    loading the product library."""
+    with np.errstate(over="ignore"):
+        s = _splitmix64(np.array([seed & _M64], dtype=np.uint64))[0]
+        idx = np.arange(n, dtype=np.uint64) + np.uint64(offset & _M64)
+        out = _splitmix64(s ^ idx)
+        k = 0
+        bad = np.nonzero(out >= np.uint64(P))[0]
+        while bad.size:
+            k += 1
+            out[bad] = _splitmix64(s ^ (idx[bad] + np.uint64((k << 48) & _M64)))
+            bad = bad[out[bad] >= np.uint64(P)]
+    return out
 
 
 def divisors():
