@@ -524,6 +524,7 @@ int gl_plan_tables(gl_plan *pl, gl_dev_tables **out) {
       if (st == GL_OK) st = upload(t, mont_powers(h_root(pl->n2, d), pl->n2, 1), &t.blk[1][d]);
       const uint64_t w = h_root(n, d);
       const uint64_t scale = d ? gl_inv(n % GL_P) : 1;
+      if (d) t.tw_unscale[d] = gl_to_mont(n % GL_P);
       if (st == GL_OK) st = upload(t, mont_powers(w, GL_TW_SPLIT, scale), &t.tw_lo[d]);
       if (st == GL_OK) st = upload(t, mont_powers(gl_pow(w, GL_TW_SPLIT), hi_count, 1), &t.tw_hi[d]);
       if (st == GL_OK && n <= kFullTwiddleMax && full_twiddles_enabled()) {
@@ -546,6 +547,7 @@ int gl_plan_tables(gl_plan *pl, gl_dev_tables **out) {
       if (st == GL_OK) st = upload(t, mont_powers(h_root(pl->n3, d), pl->n3, 1), &t.blk3[d]);
       const uint64_t w = h_root(n, d);
       const uint64_t scale = d ? gl_inv(n % GL_P) : 1;
+      if (d) t.tw_unscale[d] = gl_to_mont(n % GL_P);
       if (st == GL_OK) st = upload(t, mont_powers(w, GL_TW_SPLIT, scale), &t.tw_lo[d]);
       if (st == GL_OK)
         st = upload(t, mont_powers(gl_pow(w, GL_TW_SPLIT), (n + GL_TW_SPLIT - 1) / GL_TW_SPLIT, 1), &t.tw_hi[d]);
@@ -919,6 +921,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       a.lanes = (uint32_t)(n23 * C);
       a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST | GL_PF_CANON_IN;
       a.tw_m = a.tw_r2 = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
+      a.tw_unscale = t->tw_unscale[d];
       a.tw_lane_div = (uint32_t)C;
       if (coset) {
         a.flags |= GL_PF_IN_TWIDDLE;
@@ -984,6 +987,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
     a.lanes = (uint32_t)(n2 * C);
     a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST | GL_PF_CANON_IN;
     a.tw_m = a.tw_r2 = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
+    a.tw_unscale = t->tw_unscale[d];
     a.tw_lane_div = (uint32_t)C;
     if (t->tw_full[d]) {
       a.flags |= GL_PF_TW_TABLE;
@@ -1055,6 +1059,7 @@ int gl_enqueue_pass_range(gl_plan *pl, int stage, const uint64_t *src, uint64_t 
     a.in_ls = a.out_ls = 1; a.in_is = a.out_is = (int64_t)n2;
     a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST | GL_PF_CANON_IN;
     a.tw_m = a.tw_r2 = t->blk[0][d]; a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
+    a.tw_unscale = t->tw_unscale[d];
     a.tw_col0 = lo;
     GL_DBG_EXTENTS(a, n1 * n2 - lo, n1 * n2 - lo);
     if (t->tw_full[d]) {

@@ -195,6 +195,7 @@ void pass_args(const poly_plan &pp, uint64_t *data, uint64_t *scratch, gl_pass_a
   a.flags = GL_PF_PASS_TWIDDLE | GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST | GL_PF_CANON_IN;
   a.tw_m = a.tw_r2 = t->blk[0][d];
   a.tw_lo = t->tw_lo[d]; a.tw_hi = t->tw_hi[d];
+  a.tw_unscale = t->tw_unscale[d];
   if (t->tw_full[d]) { a.flags |= GL_PF_TW_TABLE; a.tw_full = t->tw_full[d]; a.tw_ld = (int64_t)n2; }
   *col = a;
   gl_pass_args b{};

@@ -99,6 +99,9 @@ struct gl_dev_tables {
   uint64_t *tw_lo[2] = {nullptr, nullptr};                          // pass twiddle, [dir]
   uint64_t *tw_hi[2] = {nullptr, nullptr};
   uint64_t *tw_full[2] = {nullptr, nullptr};  // omega_n^(col*k) at [k*n2 + col], [dir]
+  // Montgomery form of the inverse of the scale tw_lo[dir] carries (n for the
+  // inverse's 1/n), 0 when unscaled (gl_pass_args::tw_unscale).
+  uint64_t tw_unscale[2] = {0, 0};
   // kind 3 only: block table of n3 and the two-level table of omega_(n2*n3).
   uint64_t *blk3[2] = {nullptr, nullptr};
   uint64_t *tw23_lo[2] = {nullptr, nullptr};

@@ -123,6 +123,7 @@ extern "C" int gl_ntt_noalloc(uint64_t *data, uint64_t len, int dir, void *strea
   a.tw_m = a.tw_r2 = tab + GL_NOALLOC_T1;
   a.tw_lo = tab + GL_NOALLOC_TLO;
   a.tw_hi = tab + GL_NOALLOC_THI;
+  a.tw_unscale = inv ? gl_to_mont(len % GL_P) : 0;  // tw_lo carries 1/len
   kc->launch(a, dim3((unsigned)gl_tiles(n2, kc)), stream);
 
   gl_pass_args b{};  // row pass: scratch -> data at the transposed position

@@ -54,6 +54,12 @@ struct gl_pass_args {
   uint64_t *const *out_ptrs;
   int32_t gen_r[3];                 // run-time radices of gl_generic_kernel
   uint64_t tw_col0;                 // pass twiddle column of lane 0 (a launch over a lane range)
+  // Montgomery form of 1/s when every tw_lo entry carries a scale s (the 1/n
+  // of an inverse transform); 0 when tw_lo is unscaled.  The pass kernels
+  // build the pass twiddle of output k = kbase + SL*t as
+  // tw(col, kbase) * omega_n^(col*SL*t), and the second factor must not
+  // carry the scale.
+  uint64_t tw_unscale;
   // Debug builds (-DGL_DEVICE_CHECKS): extents, in words from `in` / `out`,
   // that every global access must stay within (0: unchecked), and the word
   // that collects GL_DBG_* bits of violations.

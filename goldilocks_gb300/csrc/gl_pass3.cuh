@@ -37,12 +37,22 @@ struct gl_p3_layout {
   static __device__ __forceinline__ int word(int c, int p) {
     return c * LS + (POW2 ? (p ^ ((p >> SH) & MSK)) : p);
   }
+  // Shared memory after the tile (words), staged during round 1 and
+  // published by the barrier that ends it:
+  //   T2    the round-2 twiddles tw_r2[R1*i], i < R2*R3 (three rounds only);
+  //   STEP  per lane c and last-round output digit t, the pass-twiddle step
+  //         omega_n^(col_c * SL * t) (SL: output stride of the last digit).
+  static constexpr int TILE = NR == 1 ? 0 : LANES * LS;
+  static constexpr int T2 = TILE;
+  static constexpr int NT2 = NR == 3 ? R2 * R3 : 0;
+  static constexpr int STEP = T2 + NT2;
+  static constexpr int NSTEP = NR == 1 ? 0 : LANES * RL;
+  static constexpr int WORDS = STEP + NSTEP;
 };
 
 template <int R1, int R2, int R3, int LANES>
 constexpr size_t gl_p3_smem_bytes() {
-  return gl_p3_layout<R1, R2, R3, LANES>::NR == 1 ? 0
-                                                   : (size_t)LANES * gl_p3_layout<R1, R2, R3, LANES>::LS * 8;
+  return (size_t)gl_p3_layout<R1, R2, R3, LANES>::WORDS * 8;
 }
 
 // One CTA's work: tile (bx, by, bz) of the pass described by `a`, with NT
@@ -137,6 +147,23 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
     }
   }
   if constexpr (L::NR == 1) return;
+  // Stage the round-2 twiddles and the pass-twiddle steps (read after the
+  // barrier below).
+  constexpr int SL = L::NR == 3 ? R1 * R2 : R1;  // output stride of the last digit
+  const bool tw_steps = (a.flags & (GL_PF_PASS_TWIDDLE | GL_PF_TW_TABLE)) == GL_PF_PASS_TWIDDLE;
+  if constexpr (L::NT2 > 0) {
+    for (int i = threadIdx.x; i < L::NT2; i += NT) gl_sm_st(a, sm, L::T2 + i, L::WORDS, __ldg(a.tw_r2 + R1 * i));
+  }
+  if (tw_steps) {
+    for (int i = threadIdx.x; i < L::NSTEP; i += NT) {
+      const int c = i / L::RL, t = i % L::RL;
+      if (lane0 + c >= (int64_t)a.lanes) continue;  // lanes past the end read no table
+      const uint64_t col = (uint64_t)(lane0 + c) / a.tw_lane_div + a.tw_col0;
+      uint64_t v = gl_tw2m(a.tw_lo, a.tw_hi, col * (uint64_t)(SL * t));
+      if (a.tw_unscale) v = gl_mont_mul(v, a.tw_unscale);
+      gl_sm_st(a, sm, L::STEP + i, L::WORDS, v);
+    }
+  }
   __syncthreads();  // uniform: every thread of the CTA reaches it
 
   // ------------------------------------------------------------- round 2
@@ -153,7 +180,7 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
 #pragma unroll
       for (int t = 0; t < R2; t++) {
         uint64_t v = x[t];
-        if (t > 0) v = gl_mont_mul(v, __ldg(a.tw_r2 + R1 * d3 * t));
+        if (t > 0) v = gl_mont_mul(v, gl_sm_ld(a, sm, L::T2 + d3 * t, L::WORDS));
         gl_sm_st(a, sm, L::word(c, base + R3 * t), LANES * L::LS, v);
       }
     }
@@ -162,8 +189,7 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
 
   // ------------------------------------------------------- last round
   {
-    constexpr int RL = L::NR == 3 ? R3 : R2;
-    constexpr int SL = L::NR == 3 ? R1 * R2 : R1;  // output stride of the last digit
+    constexpr int RL = L::RL;
     constexpr int G = M / RL;                      // groups: (k1, k2) or k1
     for (int idx = threadIdx.x; idx < LANES * G; idx += NT) {
       int c, g;
@@ -187,7 +213,16 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
       const int64_t lane = lane0 + c;
       if (lane < (int64_t)a.lanes) {
         uint64_t *dst = out + lane * a.out_ls;
-        if (a.flags & GL_PF_PASS_TWIDDLE) {
+        if (tw_steps) {
+          // tw(col, kbase + SL*t) = tw(col, kbase) * omega_n^(col*SL*t).
+          const uint64_t col = (uint64_t)lane / a.tw_lane_div + a.tw_col0;
+          const uint64_t base = gl_tw2m(a.tw_lo, a.tw_hi, col * (uint64_t)kbase);
+#pragma unroll
+          for (int t = 0; t < RL; t++) {
+            const uint64_t tw = t == 0 ? base : gl_mont_mul(base, gl_sm_ld(a, sm, L::STEP + c * RL + t, L::WORDS));
+            gl_st_out(a, dst + (int64_t)(kbase + SL * t) * a.out_is, gl_mont_mul(x[t], tw));
+          }
+        } else if (a.flags & GL_PF_PASS_TWIDDLE) {
           const uint64_t col = (uint64_t)lane / a.tw_lane_div;
 #pragma unroll
           for (int t = 0; t < RL; t++) {

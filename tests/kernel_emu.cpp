@@ -33,6 +33,7 @@ uint64_t sm[1 << 16];  // the CTA's dynamic shared memory
 #define atomicOr(p, v) __atomic_fetch_or((p), (v), __ATOMIC_RELAXED)
 static uint64_t g_dbg_in = 0, g_dbg_out = 0;
 static uint32_t g_dbg_err = 0;
+static uint64_t g_tw_unscale = 0;  // gl_pass_args::tw_unscale of the next launches
 
 #include "gl_pass3.cuh"
 #include "gl_generic.cuh"
@@ -106,6 +107,7 @@ int emu_pass3(EMU_ARGS) {
   a.tw_lane_div = tw_lane_div; a.in_limit = in_limit;
   a.itw_lo = itw_lo; a.itw_hi = itw_hi; a.itw_jmul = itw_jmul;
   a.dbg_in_words = g_dbg_in; a.dbg_out_words = g_dbg_out; a.dbg_err = &g_dbg_err;
+  a.tw_unscale = g_tw_unscale;
   const unsigned gx = (lanes + 3) / 4;
 #define SHAPE(R1, R2, R3, NT)                                                        \
   if (r1 == R1 && r2 == R2 && r3 == R3) {                                              \
@@ -130,6 +132,10 @@ void emu_set_checks(uint64_t in_words, uint64_t out_words) {
   g_dbg_in = in_words;
   g_dbg_out = out_words;
 }
+
+// Montgomery form of the inverse of the scale the next launches' tw_lo
+// carries (0: unscaled).
+void emu_set_unscale(uint64_t v) { g_tw_unscale = v; }
 
 // GL_DBG_* bits of the violations since the last call, then cleared.
 uint32_t emu_check_flags() {

@@ -26,6 +26,7 @@ def build_emu(tmp_path_factory, extra=()):
     lib = ctypes.CDLL(str(so))
     lib.emu_set_checks.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
     lib.emu_check_flags.restype = ctypes.c_uint32
+    lib.emu_set_unscale.argtypes = [ctypes.c_uint64]
     vp, i64, u32, u64 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint64
     for f in (lib.emu_pass3, lib.emu_generic):
         f.argtypes = [ctypes.c_int] * 4 + [vp, vp, i64, i64, i64, i64, u32, u32,
@@ -60,10 +61,13 @@ def table(w, count, scale=1):
 
 
 def call(emu, shape, inv, x, out, in_ls, in_is, out_ls, out_is, lanes, flags, tw_m, tw_r2,
-         tw_lo=None, tw_hi=None, lane_div=1, in_limit=NOLIM, itw_lo=None, itw_hi=None, jmul=0):
+         tw_lo=None, tw_hi=None, lane_div=1, in_limit=NOLIM, itw_lo=None, itw_hi=None, jmul=0,
+         unscale=1):
     """`shape` = (r1, r2, r3) of a compiled kernel, or ("gen", r1, r2, r3) for
-    the run-time-radix kernel."""
+    the run-time-radix kernel.  `unscale` is the inverse of the scale tw_lo
+    carries (1: unscaled)."""
     ptr = lambda a: None if a is None else a.ctypes.data
+    emu.emu_set_unscale(0 if unscale == 1 else unscale * 2**64 % P)
     fn = emu.emu_pass3
     if shape[0] == "gen":
         fn, shape = emu.emu_generic, shape[1:]
@@ -109,7 +113,7 @@ def four_step(emu, n1, n2, shape1, shape2, x, inv=False, C=1, in_limit=NOLIM, co
         kw = dict(in_limit=in_limit, itw_lo=table(g, 4096), itw_hi=table(pow(g, 4096, P), 64), jmul=n2)
         flags |= F_IN_TW
     call(emu, shape1, inv, x, scratch, 1, n2 * C, 1, n2 * C, n2 * C, flags, t1, t1, lo, hi,
-         lane_div=C, **kw)
+         lane_div=C, unscale=n if inv else 1, **kw)
     assert C == 1
     call(emu, shape2, inv, scratch, out, n2, 1, 1, n1, n1, F_STORE_LF, t2, t2)
     return out
@@ -129,7 +133,8 @@ def three_step(emu, n1, n2, n3, shapes, x, inv=False):
     lo23, hi23 = table(w23, 4096), table(pow(w23, 4096, P), (n23 + 4095) // 4096)
     t1, t2, t3 = table(root(n1, inv), n1), table(root(n2, inv), n2), table(root(n3, inv), n3)
     flags = F_PASS_TW | F_LOAD_LF | F_STORE_LF
-    call(emu, shapes[0], inv, x, s1, 1, n23, 1, n23, n23, flags | F_CANON_IN, t1, t1, lo, hi)
+    call(emu, shapes[0], inv, x, s1, 1, n23, 1, n23, n23, flags | F_CANON_IN, t1, t1, lo, hi,
+         unscale=n if inv else 1)
     for k1 in range(n1):  # grid.y of the middle pass: one n23 block per k1, in place
         blk = s1[k1 * n23:(k1 + 1) * n23]
         call(emu, shapes[1], inv, blk, blk, 1, n3, 1, n3, n3, flags, t2, t2, lo23, hi23)
