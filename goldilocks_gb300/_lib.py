@@ -39,6 +39,7 @@ SIGNATURES = [
     ("gl_host_pipeline", _int, [_vp, _u64, _u32]),
     ("gl_batch_wait_selftest", _int, [_u64, ctypes.POINTER(_u32)]),
     ("gl_debug_inject_alloc_failures", _int, [_int]),
+    ("gl_debug_field_op", _int, [_int, _vp, _vp, _vp, _u64, _vp]),
     ("gl_debug_checks_enabled", _int, []),
     ("gl_debug_check_status", _int, [ctypes.POINTER(_u32)]),
     ("gl_k12_next_layer_size", _u64, [_u64]),
@@ -60,6 +61,7 @@ SIGNATURES = [
     ("gl_server_submit", _int, [_vp, _vp, ctypes.POINTER(_u64)]),
     ("gl_server_poll", _int, [_vp, _u64, ctypes.POINTER(_int)]),
     ("gl_server_wait", _int, [_vp, _u64, _int, ctypes.POINTER(_int)]),
+    ("gl_server_wait_timed", _int, [_vp, _u64, _int, ctypes.POINTER(_int), ctypes.POINTER(ctypes.c_double)]),
     ("gl_server_cancel", _int, [_vp, _u64]),
     ("gl_server_get_stats", _int, [_vp, _vp]),
     ("gl_server_destroy", _int, [_vp]),
@@ -119,6 +121,7 @@ GL_ERR_NOT_FOUND = 9
 GL_ERR_IO = 10
 GL_ERR_VERIFY = 11
 GL_FORWARD, GL_INVERSE = 0, 1
+GL_FOP_ADD, GL_FOP_SUB, GL_FOP_CANON, GL_FOP_MONT_MUL, GL_FOP_MUL, GL_FOP_SHL = 0, 1, 3, 4, 5, 100
 GL_MEM_HOST, GL_MEM_DEVICE = 0, 1
 
 _lib = None

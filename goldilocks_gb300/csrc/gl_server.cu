@@ -1,15 +1,22 @@
 // Continuous-batching request server for NTT / inverse NTT / coset LDE jobs
 // on device-resident data (no counterpart in the reference).
 //
-// Requests are queued by gl_server_submit from any thread.  A scheduler
-// thread admits queued requests in arrival order while the device memory they
+// Requests are queued by gl_server_submit from any thread, in two classes:
+// small (at most kSmallWords output words) and large.  A scheduler thread
+// admits each class in arrival order while the device memory the requests
 // need (the temporaries the server allocates: scratch, LDE coefficients) fits
-// the budget, groups the admitted ones into a batch and launches it on a free
-// slot -- one CUDA stream per slot -- so batches run concurrently on the GPU:
-//   * single-column NTT/iNTT jobs of the batch go to one persistent-kernel
-//     launch (gl_batch.cu); sizes it is not built for run as plain calls;
-//   * multi-column jobs run as column-batched transforms (gl_ntt_columns path);
-//   * LDE jobs run gl_coset_lde.
+// the budget, and launches them on free slots -- one CUDA stream per slot --
+// so that work of several slots runs concurrently on the GPU:
+//   * slot 0 (when there are two slots or more) takes small requests only,
+//     on a stream of the highest priority: the block scheduler starts its
+//     CTAs ahead of the large requests' CTAs that are waiting, so a small
+//     request never waits for a large one to finish, only for running CTAs;
+//   * the other slots take one large request at a time (low priority), or,
+//     with no large request waiting, a batch of small ones;
+//   * a batch's single-column NTT/iNTT jobs go to one persistent-kernel
+//     launch (gl_batch.cu); other NTT/iNTT jobs are transformed out of place
+//     from the request's input to its output (no copy first); LDE jobs run
+//     gl_coset_lde.
 // A host function queued after the batch on its stream marks completion;
 // memory returns to the budget and waiters wake.  Requests that arrive while
 // batches are in flight are admitted as slots and memory free up.  Every wait
@@ -47,6 +54,7 @@ struct job {
 struct slot {
   cudaStream_t stream = nullptr;
   bool busy = false;
+  bool small_only = false;  // reserved for small requests (highest priority)
   std::vector<std::shared_ptr<job>> jobs;
   uint32_t *err = nullptr;  // pinned: persistent kernel error word
   int launch_status = GL_OK;
@@ -63,7 +71,8 @@ struct gl_server {
   std::mutex mu;
   std::condition_variable cv;       // scheduler wake-ups
   std::condition_variable done_cv;  // waiter wake-ups
-  std::deque<std::shared_ptr<job>> queue;
+  std::deque<std::shared_ptr<job>> queue;        // large requests
+  std::deque<std::shared_ptr<job>> small_queue;  // small requests
   std::map<uint64_t, std::shared_ptr<job>> jobs;
   uint64_t next_id = 1;
   bool stop = false;
@@ -77,6 +86,11 @@ struct gl_server {
 namespace {
 
 uint64_t out_rows(const gl_request &r) { return r.op == GL_OP_LDE ? r.n * r.blowup : r.n; }
+
+// Requests with at most this many output words are small: a few passes of at
+// most 16 MiB each, tens of microseconds on the GPU.
+constexpr uint64_t kSmallWords = 1ull << 21;
+bool is_small(const gl_request &r) { return out_rows(r) * r.cols <= kSmallWords; }
 
 // Device bytes the server allocates for the request (its temporaries).
 int footprint(const gl_request &r, uint64_t *bytes) {
@@ -113,41 +127,45 @@ int launch_batch(gl_server *s, int si, std::vector<std::shared_ptr<job>> &batch)
   cudaStream_t st = sl.stream;
   std::vector<gl_poly> polys;
   int rc = GL_OK;
+  // Single-column transforms go to the persistent kernel when the batch has
+  // more than kDirectMax of them.
+  size_t singles = 0;
+  for (auto &j : batch) singles += j->req.op != GL_OP_LDE && j->req.cols == 1;
+  const bool persistent = singles > kDirectMax;
   for (auto &j : batch) {
     const gl_request &r = j->req;
     if (r.op == GL_OP_LDE) {
       rc = gl_coset_lde(r.in, r.out, r.n, r.cols, r.blowup, r.shift, GL_MEM_DEVICE, st);
-    } else {
-      const uint64_t words = r.n * r.cols;
+    } else if (persistent && r.cols == 1) {
+      // In place on the output.
       if (r.out != r.in) {
-        cudaError_t e = cudaMemcpyAsync(r.out, r.in, words * 8, cudaMemcpyDeviceToDevice, st);
+        cudaError_t e = cudaMemcpyAsync(r.out, r.in, r.n * 8, cudaMemcpyDeviceToDevice, st);
         if (e != cudaSuccess) rc = gl_cuda_status(e);
       }
+      if (rc == GL_OK) polys.push_back({r.out, r.n, r.op == GL_OP_INTT ? GL_INVERSE : GL_FORWARD, 0});
+    } else {
+      // Out of place: the first pass reads the input, the last writes the
+      // output (the plan's scratch holds what lies between).
+      gl_plan *pl = nullptr;
+      rc = gl_plan_create(r.n, &pl);
+      void *scratch = nullptr;
+      const uint64_t sw = rc == GL_OK ? gl_plan_scratch_words(pl, r.cols, 1) : 0;
+      if (rc == GL_OK && sw) rc = gl_cuda_status(gl_malloc_async(&scratch, sw * 8, st));
       if (rc == GL_OK) {
-        if (r.cols == 1) {
-          polys.push_back({r.out, r.n, r.op == GL_OP_INTT ? GL_INVERSE : GL_FORWARD, 0});
-        } else if (!(r.op == GL_OP_INTT && r.n == 1)) {
-          rc = gl_ntt_columns(r.out, r.n, r.cols, r.op == GL_OP_INTT ? GL_INVERSE : GL_FORWARD,
-                              GL_MEM_DEVICE, st);
+        if (r.op == GL_OP_INTT && r.n == 1) {
+          if (r.out != r.in)
+            rc = gl_cuda_status(cudaMemcpyAsync(r.out, r.in, r.cols * 8, cudaMemcpyDeviceToDevice, st));
+        } else {
+          rc = gl_enqueue_transform(pl, r.in, r.out, r.cols, 1, r.n * r.cols, r.op == GL_OP_INTT,
+                                    (uint64_t *)scratch, st);
         }
       }
+      if (scratch) cudaFreeAsync(scratch, st);
     }
     if (rc != GL_OK) break;
   }
   *sl.err = 0;
-  if (rc == GL_OK && !polys.empty()) {
-    if (polys.size() <= kDirectMax) {
-      // A lone request: plain launches on the slot's stream; the persistent
-      // kernel's work-list upload would cost more than it saves.
-      for (const gl_poly &p : polys) {
-        rc = p.dir == GL_INVERSE ? gl_intt(p.data, p.len, GL_MEM_DEVICE, st)
-                                 : gl_ntt(p.data, p.len, GL_MEM_DEVICE, st);
-        if (rc != GL_OK) break;
-      }
-    } else {
-      rc = gl_batch_enqueue_persistent(polys.data(), polys.size(), st, sl.err);
-    }
-  }
+  if (rc == GL_OK && !polys.empty()) rc = gl_batch_enqueue_persistent(polys.data(), polys.size(), st, sl.err);
   sl.launch_status = rc;
   done_ctx *ctx = new done_ctx{s, si};
   cudaError_t e = cudaLaunchHostFunc(st, on_batch_done, ctx);
@@ -192,22 +210,29 @@ void scheduler(gl_server *s) {
   cudaSetDevice(s->device);
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
-    // Find a free slot and the jobs to admit.
-    int free_slot = -1;
-    for (size_t i = 0; i < s->slots.size(); i++)
-      if (!s->slots[i].busy) { free_slot = (int)i; break; }
-    std::vector<std::shared_ptr<job>> batch;
-    if (free_slot >= 0) {
-      while (!s->queue.empty() && (int)batch.size() < s->max_batch) {
-        auto &j = s->queue.front();
-        if (j->status == GL_ERR_CANCELLED) { s->queue.pop_front(); continue; }
+    // Admit from `q` in arrival order, up to `limit` jobs, while memory fits.
+    auto admit = [&](std::deque<std::shared_ptr<job>> &q, int limit,
+                     std::vector<std::shared_ptr<job>> &batch) {
+      while (!q.empty() && (int)batch.size() < limit) {
+        auto &j = q.front();
+        if (j->status == GL_ERR_CANCELLED) { q.pop_front(); continue; }
         if (s->in_use + j->bytes > s->budget) break;  // arrival order: wait for memory
         s->in_use += j->bytes;
         s->max_in_use = std::max(s->max_in_use, s->in_use);
         j->launched = true;
         batch.push_back(j);
-        s->queue.pop_front();
+        q.pop_front();
       }
+    };
+    // A free slot and the jobs to admit on it: the reserved slot takes small
+    // requests; the others a large request, else small ones.
+    int free_slot = -1;
+    std::vector<std::shared_ptr<job>> batch;
+    for (size_t i = 0; i < s->slots.size() && batch.empty(); i++) {
+      if (s->slots[i].busy) continue;
+      if (!s->slots[i].small_only) admit(s->queue, 1, batch);
+      if (batch.empty()) admit(s->small_queue, s->max_batch, batch);
+      if (!batch.empty()) free_slot = (int)i;
     }
     if (!batch.empty()) {
       slot &sl = s->slots[free_slot];
@@ -227,7 +252,7 @@ void scheduler(gl_server *s) {
     }
     bool idle = true;
     for (auto &sl : s->slots) idle = idle && !sl.busy;
-    if (s->stop && s->queue.empty() && idle) break;
+    if (s->stop && s->queue.empty() && s->small_queue.empty() && idle) break;
     s->cv.wait_for(lk, std::chrono::milliseconds(50));
   }
 }
@@ -244,8 +269,12 @@ extern "C" int gl_server_create(uint64_t budget_bytes, int slots, int max_batch,
   if (e != cudaSuccess) { delete s; return gl_cuda_status(e); }
   gl_init_mempool_once();
   s->slots.resize(slots);
+  int prio_low = 0, prio_high = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+  if (slots >= 2) s->slots[0].small_only = true;
   for (auto &sl : s->slots) {
-    e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+    e = cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking,
+                                     sl.small_only ? prio_high : prio_low);
     if (e == cudaSuccess) e = cudaMallocHost(&sl.err, sizeof(uint32_t));
     if (e != cudaSuccess) {
       for (auto &x : s->slots) {
@@ -284,7 +313,7 @@ extern "C" int gl_server_submit(gl_server *s, const gl_request *req, uint64_t *i
   j->bytes = bytes;
   j->t_submit = clk::now();
   s->jobs[j->id] = j;
-  s->queue.push_back(j);
+  (is_small(j->req) ? s->small_queue : s->queue).push_back(j);
   s->submitted++;
   *id = j->id;
   s->cv.notify_all();
@@ -301,6 +330,11 @@ extern "C" int gl_server_poll(gl_server *s, uint64_t id, int *status) {
 }
 
 extern "C" int gl_server_wait(gl_server *s, uint64_t id, int timeout_ms, int *status) {
+  return gl_server_wait_timed(s, id, timeout_ms, status, nullptr);
+}
+
+extern "C" int gl_server_wait_timed(gl_server *s, uint64_t id, int timeout_ms, int *status,
+                                    double *latency_ms) {
   if (!s || !status) return GL_ERR_INVALID;
   std::unique_lock<std::mutex> lk(s->mu);
   auto it = s->jobs.find(id);
@@ -310,6 +344,10 @@ extern "C" int gl_server_wait(gl_server *s, uint64_t id, int timeout_ms, int *st
                                         [&] { return j->status != GL_ERR_BUSY; });
   if (!done) return GL_ERR_TIMEOUT;
   *status = j->status;
+  if (latency_ms)  // 0 for a request cancelled before launch
+    *latency_ms = j->status == GL_ERR_CANCELLED
+                      ? 0.0
+                      : std::chrono::duration<double, std::milli>(j->t_done - j->t_submit).count();
   s->jobs.erase(id);  // the result has been delivered
   return GL_OK;
 }

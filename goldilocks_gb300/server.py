@@ -53,11 +53,15 @@ class Server:
         return s.value
 
     def wait(self, rid, timeout_ms=60000):
-        s = ctypes.c_int()
-        st = self._lib.gl_server_wait(self._h, rid, timeout_ms, ctypes.byref(s))
+        return self.wait_timed(rid, timeout_ms)[0]
+
+    def wait_timed(self, rid, timeout_ms=60000):
+        """(status, submit-to-completion milliseconds) of a request."""
+        s, lat = ctypes.c_int(), ctypes.c_double()
+        st = self._lib.gl_server_wait_timed(self._h, rid, timeout_ms, ctypes.byref(s), ctypes.byref(lat))
         if st != L.GL_OK:
             raise GoldilocksError(st, "wait")
-        return s.value
+        return s.value, lat.value
 
     def cancel(self, rid):
         return self._lib.gl_server_cancel(self._h, rid)
@@ -144,50 +148,85 @@ class _Ring:
         return self.buf[start:end], start, end
 
 
-def serve_stream(reqs, arrivals, pool, budget_bytes=64 << 30, slots=4, max_batch=64, ring_words=0):
+def _percentiles(lat_ms):
+    v = sorted(lat_ms)
+    if not v:
+        return {"p50_ms": 0.0, "p99_ms": 0.0, "max_ms": 0.0}
+    q = lambda f: v[min(len(v) - 1, int(f * len(v)))]
+    return {"p50_ms": q(0.50), "p99_ms": q(0.99), "max_ms": v[-1]}
+
+
+def serve_stream(reqs, arrivals, pool, budget_bytes=64 << 30, slots=4, max_batch=64, ring_words=0,
+                 keep=()):
     """Submit each request at its arrival time (seconds from start), wait for
-    all; returns (elements/s, stats, wall seconds, outputs).  With ring_words
-    > 0 the outputs share a ring of that many words: each returned output is
-    a view of the ring, which a later request may have overwritten."""
+    all; returns (elements/s, stats, wall seconds, outputs).  stats adds to the
+    server's counters each request's latency from its arrival to its
+    completion (`latency_ms`, and p50/p99 of it).  With ring_words > 0 the
+    outputs share a ring of that many words: each returned output is a view of
+    the ring, which a later request may have overwritten -- except the
+    requests whose indices are in `keep`, which get buffers of their own."""
     import torch
+    keep = set(keep)
     if ring_words:
         ins, outs, ring = [pool[:n * c] for _, n, c, _ in reqs], [], _Ring(torch, ring_words)
+        own = {k: torch.empty(_out_words(*reqs[k]), dtype=torch.int64, device="cuda") for k in sorted(keep)}
     else:
-        (ins, outs), ring = _buffers(torch, reqs, pool), None
+        (ins, outs), ring, own = _buffers(torch, reqs, pool), None, {}
     torch.cuda.synchronize()
-    pending = collections.OrderedDict()
+    pending = collections.OrderedDict()  # rid -> (request index, submit time)
+    lat = [0.0] * len(reqs)
     with Server(budget_bytes, slots, max_batch) as srv:
         def wait(rid):
-            st = srv.wait(rid, timeout_ms=600000)
-            pending.pop(rid, None)
+            k, t_sub = pending.pop(rid)
+            st, ms = srv.wait_timed(rid, timeout_ms=600000)
             if st != L.GL_OK:
                 raise GoldilocksError(st, "request")
+            lat[k] = (t_sub - arrivals[k]) * 1e3 + ms  # from arrival, not from submission
         t0 = time.perf_counter()
         for k, ((op, n, cols, blowup), a, i) in enumerate(zip(reqs, arrivals, ins)):
             now = time.perf_counter() - t0
             if a > now:
                 time.sleep(a - now)
-            if ring:
+            if k in own:
+                o = own[k]
+                outs.append(o)
+            elif ring:
                 o, lo, hi = ring.take(_out_words(op, n, cols, blowup), wait)
                 outs.append(o)
             else:
                 o = outs[k]
+            t_sub = time.perf_counter() - t0
             rid = srv.submit(op, n, cols, i, o, blowup)
-            pending[rid] = True
-            if ring:
+            pending[rid] = (k, max(t_sub, float(a)))
+            if ring and k not in own:
                 ring.live.append((rid, lo, hi))
         for rid in list(pending):
             wait(rid)
         wall = time.perf_counter() - t0
         stats = srv.stats()
+    stats["latency_ms"] = lat
+    stats.update({"arrival_" + k: v for k, v in _percentiles(lat).items()})
     elements = sum(n * cols for _, n, cols, _ in reqs)
     return elements / wall, stats, wall, outs
 
 
+def plain_call(lib, stream, op, n, cols, blowup, inp, out):
+    """One request through the plain per-call API: gl_coset_lde, or a copy
+    and the in-place column transform (the reference's ntt/intt are in place)."""
+    if op == GL_OP_LDE:
+        return lib.gl_coset_lde(inp.data_ptr(), out.data_ptr(), n, cols, blowup, 7, L.GL_MEM_DEVICE, stream)
+    out.copy_(inp)
+    d = L.GL_INVERSE if op == GL_OP_INTT else L.GL_FORWARD
+    return lib.gl_ntt_columns(out.data_ptr(), n, cols, d, L.GL_MEM_DEVICE, stream)
+
+
 def serial_baseline(reqs, pool, ring_words=0):
     """The same requests one at a time through the plain API (gl_ntt_columns,
-    gl_coset_lde, gl_ntt/gl_intt), each synchronised before the next starts.
-    With ring_words > 0 every output reuses one buffer (no outputs returned)."""
+    gl_coset_lde), each synchronised before the next starts.  Returns
+    (elements/s, latency percentiles, wall seconds, outputs); the latencies
+    are service times (no queueing), also listed per request as
+    `service_ms`.  With ring_words > 0 every output reuses one buffer (no
+    outputs returned)."""
     import torch
     lib = L.load()
     if ring_words:
@@ -202,27 +241,134 @@ def serial_baseline(reqs, pool, ring_words=0):
     for k, ((op, n, cols, blowup), i) in enumerate(zip(reqs, ins)):
         o = outs[k] if outs is not None else scratch[:_out_words(op, n, cols, blowup)]
         t = time.perf_counter()
-        if op == GL_OP_LDE:
-            st = lib.gl_coset_lde(i.data_ptr(), o.data_ptr(), n, cols, blowup, 7, L.GL_MEM_DEVICE, stream)
-        else:
-            o.copy_(i)
-            d = L.GL_INVERSE if op == GL_OP_INTT else L.GL_FORWARD
-            st = lib.gl_ntt_columns(o.data_ptr(), n, cols, d, L.GL_MEM_DEVICE, stream)
+        st = plain_call(lib, stream, op, n, cols, blowup, i, o)
         if st != L.GL_OK:
             raise GoldilocksError(st, "serial")
         torch.cuda.synchronize()
         lat.append((time.perf_counter() - t) * 1e3)
     wall = time.perf_counter() - t0
     elements = sum(n * cols for _, n, cols, _ in reqs)
-    lat.sort()
-    return elements / wall, {"p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))]}, wall, outs
+    pct = _percentiles(lat)
+    pct["service_ms"] = lat
+    return elements / wall, pct, wall, outs
+
+
+def serial_fifo(service_ms, arrivals):
+    """Latencies of the serial path under the same arrivals: one request at a
+    time in arrival order (a single FIFO server), request k taking its
+    measured serial service time: finish_k = max(arrival_k, finish_(k-1)) +
+    service_k.  Returns (latency percentiles and per-request latencies, wall
+    seconds from the first arrival to the last finish)."""
+    finish, lat = 0.0, []
+    for a, s in zip(arrivals, service_ms):
+        finish = max(float(a), finish) + s * 1e-3
+        lat.append((finish - float(a)) * 1e3)
+    pct = _percentiles(lat)
+    pct["latency_ms"] = lat
+    return pct, finish - float(arrivals[0]) if len(arrivals) else 0.0
+
+
+def check_sample(reqs, count, seed, max_words):
+    """Indices of requests whose served outputs are kept and checked: the
+    largest request of each operation, then a seeded sample, while the kept
+    outputs total at most max_words."""
+    rng = np.random.default_rng(seed)
+    order = []
+    for op in (GL_OP_LDE, GL_OP_NTT, GL_OP_INTT):
+        ks = [k for k, r in enumerate(reqs) if r[0] == op]
+        if ks:
+            order.append(max(ks, key=lambda k: _out_words(*reqs[k])))
+    order += [int(k) for k in rng.permutation(len(reqs))]
+    chosen, words = [], 0
+    for k in order:
+        w = _out_words(*reqs[k])
+        if k in chosen or words + w > max_words:
+            continue
+        chosen.append(k)
+        words += w
+        if len(chosen) >= count:
+            break
+    return sorted(chosen)
+
+
+def check_outputs(reqs, pool, outs, indices):
+    """Compare served outputs with the plain per-call API's result for the
+    same request (ntt/src/ntt/mod.rs:98-120 restated on the GPU: the path the
+    GPU tests check against the oracle), bit for bit, on the device.  Returns
+    the indices that differ."""
+    import torch
+    lib = L.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    bad = []
+    for k in indices:
+        op, n, cols, blowup = reqs[k]
+        ref = torch.empty(_out_words(op, n, cols, blowup), dtype=torch.int64, device="cuda")
+        st = plain_call(lib, stream, op, n, cols, blowup, pool[:n * cols], ref)
+        if st != L.GL_OK:
+            raise GoldilocksError(st, "check")
+        if not torch.equal(ref, outs[k]):
+            bad.append(k)
+        del ref
+    torch.cuda.synchronize()
+    return bad
+
+
+def compare_at_loads(reqs, pool, loads, seed, budget_bytes=64 << 30, slots=4, max_batch=64,
+                     ring_words=0, check=0, check_words=0, p99_bound=2.0):
+    """The serving comparison: serial plain calls back to back (service
+    times), then for each offered load (a multiple of the rate the serial path
+    sustains) the served stream at those Poisson arrivals beside the serial
+    path under the same arrivals (a FIFO queue of the measured service times).
+    With check > 0, that many served outputs per load (seeded sample,
+    including the largest request of each operation) are compared with the
+    plain call's.  Reports elements/s and p50/p99 latency from arrival, and
+    the best served rate whose p99 is within p99_bound times the serial
+    p99 at the same load."""
+    ser_rate, ser_lat, ser_wall, _ = serial_baseline(reqs, pool, ring_words=ring_words or 1)
+    elements = sum(n * c for _, n, c, _ in reqs)
+    small = [k for k, r in enumerate(reqs) if _out_words(*r) <= 1 << 21]
+    res = {"requests": len(reqs), "elements": elements,
+           "serial": {"elem_s": ser_rate, "wall_s": ser_wall, "service_p50_ms": ser_lat["p50_ms"],
+                      "service_p99_ms": ser_lat["p99_ms"]},
+           "loads": [], "checked": 0, "mismatches": []}
+    offered = len(reqs) / ser_wall  # requests/s the serial path sustains
+    for load in loads:
+        arrivals = poisson_arrivals(len(reqs), rate_per_s=offered * load, seed=seed)
+        fifo, fifo_wall = serial_fifo(ser_lat["service_ms"], arrivals)
+        keep = check_sample(reqs, check, seed + int(load * 1000), check_words) if check else []
+        rate, stats, wall, outs = serve_stream(reqs, arrivals, pool, budget_bytes=budget_bytes, slots=slots,
+                                               max_batch=max_batch, ring_words=ring_words, keep=keep)
+        if keep:
+            res["mismatches"] += [int(k) for k in check_outputs(reqs, pool, outs, keep)]
+            res["checked"] += len(keep)
+        del outs
+        sl = stats["latency_ms"]
+        entry = {"load": load, "offered_req_s": offered * load,
+                 "served": {"elem_s": rate, "wall_s": wall, "p50_ms": stats["arrival_p50_ms"],
+                            "p99_ms": stats["arrival_p99_ms"], "batches": stats["batches"],
+                            "small_p99_ms": _percentiles([sl[k] for k in small])["p99_ms"]},
+                 "serial_same_arrivals": {"elem_s": elements / fifo_wall if fifo_wall else 0.0,
+                                          "p50_ms": fifo["p50_ms"], "p99_ms": fifo["p99_ms"],
+                                          "small_p99_ms": _percentiles([fifo["latency_ms"][k] for k in small])["p99_ms"]}}
+        res["loads"].append(entry)
+    ok = [e for e in res["loads"] if e["served"]["p99_ms"] <= p99_bound * e["serial_same_arrivals"]["p99_ms"]]
+    best = max(ok, key=lambda e: e["served"]["elem_s"]) if ok else None
+    res["p99_bound"] = "served p99 <= %g x serial p99 at the same arrivals" % p99_bound
+    res["best_within_bound"] = None if best is None else {
+        "load": best["load"], "served_elem_s": best["served"]["elem_s"],
+        "serial_elem_s_same_arrivals": best["serial_same_arrivals"]["elem_s"],
+        "serial_elem_s_back_to_back": ser_rate,
+        "served_p99_ms": best["served"]["p99_ms"], "serial_p99_ms": best["serial_same_arrivals"]["p99_ms"]}
+    return res
 
 
 def main(argv=None):
     """The serving workload at full size: NTT/iNTT/LDE (40/30/30, blowup 4,
     shift 7), log2 n uniform in [10, 24], 1..64 columns, Poisson arrivals at
-    0.5x and 2x the rate the serial path sustains, a 64 GB admission budget;
-    outputs share a ring (default 96 GiB).  Prints one JSON line."""
+    multiples of the rate the serial path sustains, a 64 GB admission budget;
+    outputs share a ring (default 96 GiB), except a seeded sample (with the
+    largest request of each operation) kept and compared bit for bit with the
+    plain per-call result.  Prints one JSON line."""
     import argparse
     import json
 
@@ -234,29 +380,22 @@ def main(argv=None):
     ap.add_argument("--log-min", type=int, default=10)
     ap.add_argument("--log-max", type=int, default=24)
     ap.add_argument("--max-cols", type=int, default=64)
-    ap.add_argument("--loads", type=str, default="0.5,2.0", help="offered load as multiples of the serial rate")
+    ap.add_argument("--loads", type=str, default="0.5,0.9,1.0,2.0",
+                    help="offered load as multiples of the serial rate")
     ap.add_argument("--ring-gib", type=int, default=96)
+    ap.add_argument("--check", type=int, default=64, help="served outputs compared per load")
+    ap.add_argument("--check-gib", type=int, default=48, help="memory for the kept outputs")
     ap.add_argument("--seed", type=int, default=0x5E77)
     args = ap.parse_args(argv)
     torch.cuda.set_device(0)
     reqs = make_requests(args.requests, seed=args.seed, log_min=args.log_min, log_max=args.log_max,
                          max_cols=args.max_cols)
     pool = torch.from_numpy(fill_uniform(max(n * c for _, n, c, _ in reqs), seed=5).view(np.int64)).cuda()
-    ring = (args.ring_gib << 30) // 8
-    ser_rate, ser_lat, ser_wall, _ = serial_baseline(reqs, pool, ring_words=ring)
-    res = {"workload": "serving", "requests": args.requests, "log2_n": [args.log_min, args.log_max],
-           "cols": [1, args.max_cols], "mix": "40/30/30 ntt/intt/lde, blowup 4", "budget_gb": 64,
-           "ring_gib": args.ring_gib, "elements": sum(n * c for _, n, c, _ in reqs),
-           "serial": {"elem_s": ser_rate, "wall_s": ser_wall, "p50_ms": ser_lat["p50_ms"],
-                      "p99_ms": ser_lat["p99_ms"]}, "served": []}
-    offered = args.requests / ser_wall
-    for load in (float(x) for x in args.loads.split(",")):
-        arrivals = poisson_arrivals(args.requests, rate_per_s=offered * load, seed=args.seed)
-        rate, stats, wall, _ = serve_stream(reqs, arrivals, pool, budget_bytes=64 << 30, slots=4,
-                                            max_batch=64, ring_words=ring)
-        res["served"].append({"offered_req_s": offered * load, "elem_s": rate, "wall_s": wall,
-                              "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"],
-                              "batches": stats["batches"]})
+    res = compare_at_loads(reqs, pool, [float(x) for x in args.loads.split(",")], args.seed,
+                           ring_words=(args.ring_gib << 30) // 8, check=args.check,
+                           check_words=(args.check_gib << 30) // 8)
+    res.update({"workload": "serving", "log2_n": [args.log_min, args.log_max], "cols": [1, args.max_cols],
+                "mix": "40/30/30 ntt/intt/lde, blowup 4", "budget_gb": 64, "ring_gib": args.ring_gib})
     print(json.dumps(res), flush=True)
 
 

@@ -263,6 +263,18 @@ void gl_tune_clear(void);
  * GL_ERR_OOM comes back and the caller's data is untouched.  0 clears it. */
 int gl_debug_inject_alloc_failures(int count);
 
+/* Device-side field primitives for tests (no counterpart in the reference):
+ * out[i] = op(a[i], b[i]) on the device, for device buffers and `stream`.
+ * GL_FOP_SHL + k multiplies a[i] by 2^k (k in 12, 24, 32, 36, 48, 64, 72,
+ * 84, 96, 108, 144; b may be null).  The results are canonical.  Operand
+ * contracts are those of gl_field.cuh: gl_add needs both operands below p,
+ * gl_sub and gl_mont_mul the second, 2^96 (a negation) its operand; the
+ * others take any words. */
+enum {
+  GL_FOP_ADD = 0, GL_FOP_SUB = 1, GL_FOP_CANON = 3, GL_FOP_MONT_MUL = 4, GL_FOP_MUL = 5, GL_FOP_SHL = 100
+};
+int gl_debug_field_op(int op, const uint64_t *a, const uint64_t *b, uint64_t *out, uint64_t n, void *stream);
+
 /* Debug builds (compiled with -DGL_DEVICE_CHECKS): the pass kernels check
  * every global and shared-memory index against the extents of their buffers;
  * a violation skips the access and sets a bit (1 input, 2 output, 4 shared
@@ -319,6 +331,9 @@ int gl_server_poll(gl_server *srv, uint64_t id, int *status);
 /* Wait up to timeout_ms for the request; GL_ERR_TIMEOUT if still pending.  On
  * return GL_OK the request is forgotten (*status holds its result). */
 int gl_server_wait(gl_server *srv, uint64_t id, int timeout_ms, int *status);
+/* gl_server_wait that also returns the request's submit-to-completion time
+ * in milliseconds (*latency_ms), for per-request latency accounting. */
+int gl_server_wait_timed(gl_server *srv, uint64_t id, int timeout_ms, int *status, double *latency_ms);
 /* Cancel a request that has not been launched yet (GL_ERR_BUSY if it has). */
 int gl_server_cancel(gl_server *srv, uint64_t id);
 int gl_server_get_stats(gl_server *srv, gl_server_stats *out);

@@ -78,6 +78,30 @@ def test_ring_outputs_and_full_mix_entry_point(gl, cuda, capsys):
             assert np.array_equal(from_dev(outs[k]), from_dev(alone[k])), (ring_words, k, reqs[k])
     _, _, _, none = S.serial_baseline(reqs, pool, ring_words=total)
     assert none is None
-    S.main(["--requests", "30", "--log-max", "12", "--max-cols", "4", "--ring-gib", "1"])
+    S.main(["--requests", "30", "--log-max", "12", "--max-cols", "4", "--ring-gib", "1", "--check", "8",
+            "--check-gib", "1"])
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
-    assert line["requests"] == 30 and len(line["served"]) == 2
+    assert line["requests"] == 30 and len(line["loads"]) == 4
+    assert line["checked"] == 4 * 8 and line["mismatches"] == []
+
+
+def test_full_size_mix_matches_requests_run_alone(gl, cuda):
+    """Requests at the configured serving sizes -- up to 2^24 rows and 64
+    columns, LDE included -- submitted together so that they overlap on the
+    GPU (large ones on the low-priority slots, small ones on the
+    high-priority one), each output equal to the plain per-call result."""
+    from goldilocks_gb300 import server as S
+    cuda.cuda.empty_cache()
+    big = [(S.GL_OP_LDE, 1 << 24, 64, 4), (S.GL_OP_NTT, 1 << 24, 64, 4), (S.GL_OP_INTT, 1 << 24, 33, 4),
+           (S.GL_OP_LDE, 1 << 22, 17, 4), (S.GL_OP_NTT, 1 << 24, 1, 4), (S.GL_OP_INTT, 1 << 23, 1, 4),
+           (S.GL_OP_LDE, 1 << 24, 1, 4), (S.GL_OP_INTT, 1 << 20, 64, 4)]
+    small = S.make_requests(28, seed=0xF5, log_min=10, log_max=18, max_cols=64)
+    reqs = [r for pair in zip(small[:len(big)], big) for r in pair] + small[len(big):]
+    pool = to_dev(cuda, gl.fill_uniform(max(n * c for _, n, c, _ in reqs), seed=0xF5))
+    arrivals = np.zeros(len(reqs))  # all at once: maximal overlap
+    _, stats, _, outs = S.serve_stream(reqs, arrivals, pool, budget_bytes=64 << 30, slots=4, max_batch=16)
+    assert stats["completed"] == len(reqs)
+    bad = S.check_outputs(reqs, pool, outs, range(len(reqs)))
+    assert bad == [], [reqs[k] for k in bad]
+    del outs, pool
+    cuda.cuda.empty_cache()
