@@ -29,19 +29,29 @@ def test_modes_match_oracle(gl, oracle, cuda, mode_name):
         assert np.array_equal(from_dev(d), want), (len(x), direction)
 
 
-def test_persistent_matches_per_call_config_shape(gl, cuda):
+def test_persistent_matches_per_call_config_shape(gl, oracle, cuda):
     """1024 polynomials, log2 n ~ U[12, 18], odd index inverse: persistent and
-    bucketed results are bit-identical to per-call results."""
+    bucketed results are bit-identical to per-call results, and a seeded
+    sample of 48 polynomials (with the longest of each direction) equals the
+    oracle in every mode."""
     from goldilocks_gb300 import batch as B
     rng = np.random.default_rng(2024)
     sizes = [1 << int(k) for k in rng.integers(12, 19, 1024)]
     outs = {}
     for mode in (B.PER_CALL, B.PERSISTENT, B.BUCKETS):
-        _, items = make_batch(cuda, sizes, seed=5)
+        xs, items = make_batch(cuda, sizes, seed=5)
         B.run(items, mode=mode)
         outs[mode] = [from_dev(d) for d, _ in items]
     for a, b, c in zip(outs[B.PER_CALL], outs[B.PERSISTENT], outs[B.BUCKETS]):
         assert np.array_equal(a, b) and np.array_equal(a, c)
+    longest = [max((i for i in range(len(sizes)) if i % 2 == d), key=lambda i: sizes[i]) for d in (0, 1)]
+    sample = sorted(set(longest) | set(rng.choice(len(sizes), 46, replace=False).tolist()))
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=8) as ex:
+        wants = list(ex.map(lambda i: oracle.intt(xs[i]) if i % 2 else oracle.ntt(xs[i]), sample))
+    for i, want in zip(sample, wants):
+        for mode in (B.PER_CALL, B.PERSISTENT, B.BUCKETS):
+            assert np.array_equal(outs[mode][i], want), (mode, i, sizes[i])
 
 
 def test_autotune_picks_a_mode(gl, cuda):
