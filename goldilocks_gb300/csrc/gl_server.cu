@@ -64,7 +64,9 @@ struct slot {
 
 struct gl_server {
   uint64_t budget = 0;
+  uint64_t small_reserve = 0;  // part of the budget only small requests use
   uint64_t in_use = 0;
+  uint64_t in_use_large = 0;   // budgeted bytes of large requests in flight
   uint64_t max_in_use = 0;
   int max_batch = 64;
   std::vector<slot> slots;
@@ -185,6 +187,7 @@ void finish_slot(gl_server *s, int si) {
     j->status = status;
     j->t_done = now;
     s->in_use -= j->bytes;
+    if (!is_small(j->req)) s->in_use_large -= j->bytes;
     s->completed++;
     s->elements += j->req.n * j->req.cols;
     s->latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - j->t_submit).count());
@@ -210,14 +213,19 @@ void scheduler(gl_server *s) {
   cudaSetDevice(s->device);
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
-    // Admit from `q` in arrival order, up to `limit` jobs, while memory fits.
+    // Admit from `q` in arrival order, up to `limit` jobs, while memory fits:
+    // large requests within the budget less the small-request reserve, small
+    // ones within the whole budget.
     auto admit = [&](std::deque<std::shared_ptr<job>> &q, int limit,
                      std::vector<std::shared_ptr<job>> &batch) {
       while (!q.empty() && (int)batch.size() < limit) {
         auto &j = q.front();
         if (j->status == GL_ERR_CANCELLED) { q.pop_front(); continue; }
+        const bool large = &q == &s->queue;
         if (s->in_use + j->bytes > s->budget) break;  // arrival order: wait for memory
+        if (large && s->in_use_large + j->bytes > s->budget - s->small_reserve) break;
         s->in_use += j->bytes;
+        if (large) s->in_use_large += j->bytes;
         s->max_in_use = std::max(s->max_in_use, s->in_use);
         j->launched = true;
         batch.push_back(j);
@@ -264,6 +272,9 @@ extern "C" int gl_server_create(uint64_t budget_bytes, int slots, int max_batch,
   *out = nullptr;
   gl_server *s = new gl_server();
   s->budget = budget_bytes;
+  // A sixteenth of the budget is kept for small requests, so that large ones
+  // holding the rest cannot make them wait for memory.
+  s->small_reserve = slots >= 2 ? budget_bytes / 16 : 0;
   s->max_batch = max_batch;
   cudaError_t e = cudaGetDevice(&s->device);
   if (e != cudaSuccess) { delete s; return gl_cuda_status(e); }
@@ -302,7 +313,7 @@ extern "C" int gl_server_submit(gl_server *s, const gl_request *req, uint64_t *i
   uint64_t bytes = 0;
   int st = footprint(*req, &bytes);
   std::lock_guard<std::mutex> lk(s->mu);
-  if (st == GL_OK && bytes > s->budget) st = GL_ERR_BUDGET;
+  if (st == GL_OK && bytes > (is_small(*req) ? s->budget : s->budget - s->small_reserve)) st = GL_ERR_BUDGET;
   if (st != GL_OK) {
     s->rejected++;
     return st;

@@ -318,13 +318,16 @@ typedef struct gl_server gl_server;
 
 /* A server on the current device with `slots` concurrent batches (one CUDA
  * stream each), at most `max_batch` requests per batch, and `budget_bytes` of
- * device memory for the temporaries of requests in flight. */
+ * device memory for the temporaries of requests in flight.  With two slots or
+ * more, slot 0 runs small requests (at most 2^21 output words) on a stream of
+ * the highest priority, and a sixteenth of the budget is reserved for them:
+ * large requests are admitted within the other fifteen sixteenths. */
 int gl_server_create(uint64_t budget_bytes, int slots, int max_batch, gl_server **out);
 /* Device bytes a request is budgeted for (scratch; LDE coefficients too). */
 int gl_server_request_bytes(const gl_request *req, uint64_t *bytes);
 /* Queue a request (thread-safe, non-blocking).  Rejected at once:
  * GL_ERR_INVALID, GL_ERR_UNSUPPORTED_SIZE, or GL_ERR_BUDGET when it needs more
- * than the whole budget. */
+ * than the budget its class may use. */
 int gl_server_submit(gl_server *srv, const gl_request *req, uint64_t *id);
 /* *status = the request's status: GL_ERR_BUSY while queued or running. */
 int gl_server_poll(gl_server *srv, uint64_t id, int *status);
