@@ -41,12 +41,14 @@ struct gl_p3_layout {
   // published by the barrier that ends it:
   //   T2    the round-2 twiddles tw_r2[R1*i], i < R2*R3 (three rounds only);
   //   STEP  per lane c and last-round output digit t, the pass-twiddle step
-  //         omega_n^(col_c * SL * t) (SL: output stride of the last digit).
+  //         omega_n^(col_c * SL * t) (SL: output stride of the last digit),
+  //         RL + 1 words per lane so that the lanes fall on distinct banks.
   static constexpr int TILE = NR == 1 ? 0 : LANES * LS;
   static constexpr int T2 = TILE;
   static constexpr int NT2 = NR == 3 ? R2 * R3 : 0;
   static constexpr int STEP = T2 + NT2;
-  static constexpr int NSTEP = NR == 1 ? 0 : LANES * RL;
+  static constexpr int SS = RL + 1;  // per-lane stride: lanes on distinct banks
+  static constexpr int NSTEP = NR == 1 ? 0 : LANES * SS;
   static constexpr int WORDS = STEP + NSTEP;
 };
 
@@ -156,7 +158,8 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
   }
   if (tw_steps) {
     for (int i = threadIdx.x; i < L::NSTEP; i += NT) {
-      const int c = i / L::RL, t = i % L::RL;
+      const int c = i / L::SS, t = i % L::SS;
+      if (t >= L::RL) continue;
       if (lane0 + c >= (int64_t)a.lanes) continue;  // lanes past the end read no table
       const uint64_t col = (uint64_t)(lane0 + c) / a.tw_lane_div + a.tw_col0;
       uint64_t v = gl_tw2m(a.tw_lo, a.tw_hi, col * (uint64_t)(SL * t));
@@ -219,7 +222,7 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
           const uint64_t base = gl_tw2m(a.tw_lo, a.tw_hi, col * (uint64_t)kbase);
 #pragma unroll
           for (int t = 0; t < RL; t++) {
-            const uint64_t tw = t == 0 ? base : gl_mont_mul(base, gl_sm_ld(a, sm, L::STEP + c * RL + t, L::WORDS));
+            const uint64_t tw = t == 0 ? base : gl_mont_mul(base, gl_sm_ld(a, sm, L::STEP + c * L::SS + t, L::WORDS));
             gl_st_out(a, dst + (int64_t)(kbase + SL * t) * a.out_is, gl_mont_mul(x[t], tw));
           }
         } else if (a.flags & GL_PF_PASS_TWIDDLE) {
