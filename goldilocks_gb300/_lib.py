@@ -40,6 +40,9 @@ SIGNATURES = [
     ("gl_batch_wait_selftest", _int, [_u64, ctypes.POINTER(_u32)]),
     ("gl_debug_inject_alloc_failures", _int, [_int]),
     ("gl_debug_field_op", _int, [_int, _vp, _vp, _vp, _u64, _vp]),
+    ("gl_preload_kernels", _int, []),
+    ("gl_transpose", _int, [_vp, _u64, _u64, _int, _vp]),
+    ("gl_bit_reverse", _int, [_vp, _u64, _int, _vp]),
     ("gl_debug_checks_enabled", _int, []),
     ("gl_debug_check_status", _int, [ctypes.POINTER(_u32)]),
     ("gl_k12_next_layer_size", _u64, [_u64]),

@@ -205,6 +205,44 @@ const gl_kernel_entry *gl_find_kernel4(uint64_t m, bool inv) {
   return generic_entry(m, inv);  // every other size up to 4096 with radices <= 17
 }
 
+__global__ void gl_fill_pass_twiddles(uint64_t *out, const uint64_t *lo, const uint64_t *hi, uint64_t n1,
+                                      uint64_t n2);
+__global__ void gl_coset_pad_kernel(const uint64_t *coef, uint64_t *dst, uint64_t n, uint64_t m,
+                                    uint64_t cols, const uint64_t *g_lo, const uint64_t *g_hi);
+
+// Under CUDA's lazy module loading (the default) a kernel's code is loaded
+// on its first launch, and that load waits for the work already running on
+// the device: the first request of a new shape would wait for a long request
+// on another stream.  Querying a kernel's attributes loads it, so this loads
+// every kernel the library can launch.
+extern "C" int gl_preload_kernels(void) {
+  GL_NVTX("gl_preload_kernels");
+  std::vector<const void *> funcs;
+  using table_fn = const gl_kernel_entry *(*)(size_t *);
+  for (table_fn f : {gl_kernels_full_fwd, gl_kernels_full_inv, gl_kernels_pass_fwd, gl_kernels_pass_inv,
+                     gl_kernels_mixed35_fwd, gl_kernels_mixed35_inv, gl_kernels_mixed17_fwd,
+                     gl_kernels_mixed17_inv, gl_kernels_pass2_fwd, gl_kernels_pass2_inv, gl_kernels_cols_fwd,
+                     gl_kernels_cols_inv}) {
+    size_t n = 0;
+    const gl_kernel_entry *e = f(&n);
+    for (size_t i = 0; i < n; i++)
+      if (e[i].func) funcs.push_back(e[i].func);
+  }
+  funcs.push_back(gl_generic_kernel_fwd());
+  funcs.push_back(gl_generic_kernel_inv());
+  funcs.push_back((const void *)gl_fill_pass_twiddles);
+  funcs.push_back((const void *)gl_coset_pad_kernel);
+  gl_batch_kernels(funcs);
+  gl_rader_kernels(funcs);
+  gl_convolve_kernels(funcs);
+  for (const void *f : funcs) {
+    cudaFuncAttributes attr;
+    cudaError_t e = cudaFuncGetAttributes(&attr, f);
+    if (e != cudaSuccess) return gl_cuda_status(e);
+  }
+  return GL_OK;
+}
+
 static std::string kernel_shape(const gl_kernel_entry *k) {
   std::string s = std::to_string(k->m) + " (" + std::to_string(k->r1) + "x" + std::to_string(k->r2);
   if (k->r3) s += "x" + std::to_string(k->r3);
@@ -453,15 +491,55 @@ static void choose_schedule(gl_plan *pl) {
   if (!gl_choice_apply(pl, c)) pl->kind = -1;  // -1: a divisor without a GPU schedule
 }
 
-static int upload(gl_dev_tables &t, const std::vector<uint64_t> &h, uint64_t **dst) {
+// Twiddle tables are built on a library stream of their own per device
+// (non-blocking, so it waits for no other stream), from the library's pool:
+// the first use of a length synchronises only that stream, never the device
+// or the caller's stream (cudaMalloc and a blocking cudaMemcpy on the legacy
+// stream can wait for every stream's work, e.g. a server slot's long
+// request).
+cudaStream_t gl_table_stream() {
+  static std::mutex mu;
+  static std::map<int, cudaStream_t> streams;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = streams.find(dev);
+  if (it != streams.end()) return it->second;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+  streams.emplace(dev, s);
+  return s;
+}
+
+int gl_table_upload(gl_dev_tables &t, const void *h, size_t bytes, void **dst) {
+  cudaStream_t s = gl_table_stream();
+  if (!s) return GL_ERR_CUDA;
   void *p = nullptr;
-  cudaError_t e = cudaMalloc(&p, h.size() * sizeof(uint64_t));
+  cudaError_t e = gl_malloc_async(&p, bytes, s);
   if (e != cudaSuccess) return gl_cuda_status(e);
-  e = cudaMemcpy(p, h.data(), h.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) { cudaFree(p); return gl_cuda_status(e); }
   t.owned.push_back(p);
-  *dst = (uint64_t *)p;
+  // Pageable source: the copy returns once the data is staged; the caller
+  // synchronises the table stream before the tables are used.
+  e = cudaMemcpyAsync(p, h, bytes, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return gl_cuda_status(e);
+  *dst = p;
   return GL_OK;
+}
+
+int gl_table_sync() { return gl_cuda_status(cudaStreamSynchronize(gl_table_stream())); }
+
+// Tables may be in use by kernels on any stream until the device is idle.
+void gl_table_free(std::vector<void *> &owned) {
+  if (owned.empty()) return;
+  cudaStream_t s = gl_table_stream();
+  cudaDeviceSynchronize();
+  for (void *p : owned) cudaFreeAsync(p, s);
+  cudaStreamSynchronize(s);
+  owned.clear();
+}
+
+static int upload(gl_dev_tables &t, const std::vector<uint64_t> &h, uint64_t **dst) {
+  return gl_table_upload(t, h.data(), h.size() * sizeof(uint64_t), (void **)dst);
 }
 
 // scale * w^i for i < count, in Montgomery form (every table the pass kernels
@@ -528,14 +606,15 @@ int gl_plan_tables(gl_plan *pl, gl_dev_tables **out) {
       if (st == GL_OK) st = upload(t, mont_powers(w, GL_TW_SPLIT, scale), &t.tw_lo[d]);
       if (st == GL_OK) st = upload(t, mont_powers(gl_pow(w, GL_TW_SPLIT), hi_count, 1), &t.tw_hi[d]);
       if (st == GL_OK && n <= kFullTwiddleMax && full_twiddles_enabled()) {
+        cudaStream_t ts = gl_table_stream();
         void *p = nullptr;
-        cudaError_t e = cudaMalloc(&p, n * sizeof(uint64_t));
+        cudaError_t e = gl_malloc_async(&p, n * sizeof(uint64_t), ts);
         if (e != cudaSuccess) { st = gl_cuda_status(e); break; }
         t.owned.push_back(p);
         t.tw_full[d] = (uint64_t *)p;
         const unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 152 * 32);
-        gl_fill_pass_twiddles<<<blocks, 256>>>(t.tw_full[d], t.tw_lo[d], t.tw_hi[d], pl->n1, pl->n2);
-        e = cudaDeviceSynchronize();
+        gl_fill_pass_twiddles<<<blocks, 256, 0, ts>>>(t.tw_full[d], t.tw_lo[d], t.tw_hi[d], pl->n1, pl->n2);
+        e = cudaGetLastError();
         if (e != cudaSuccess) st = gl_cuda_status(e);
       }
     }
@@ -558,8 +637,9 @@ int gl_plan_tables(gl_plan *pl, gl_dev_tables **out) {
                     &t.tw23_hi[d]);
     }
   }
+  if (st == GL_OK) st = gl_table_sync();  // the tables are complete before any use
   if (st != GL_OK) {
-    for (void *p : t.owned) cudaFree(p);
+    gl_table_free(t.owned);
     return st;
   }
   auto res = pl->dev.emplace(dev, std::move(t));
@@ -643,7 +723,7 @@ gl_plan *gl_plan_from_choice(uint64_t size, const gl_choice &c) {
 void gl_plan_free(gl_plan *pl) {
   if (!pl) return;
   for (auto &kv : pl->dev)
-    for (void *p : kv.second.owned) cudaFree(p);
+    gl_table_free(kv.second.owned);
   delete pl;
 }
 
@@ -1096,7 +1176,9 @@ cudaError_t gl_malloc_async(void **p, size_t bytes, cudaStream_t stream) {
       return cudaErrorMemoryAllocation;
     }
   }
-  return cudaMallocAsync(p, bytes, stream);
+  cudaMemPool_t pool = gl_mempool();
+  if (!pool) return cudaErrorMemoryAllocation;
+  return cudaMallocFromPoolAsync(p, bytes, pool, stream);
 }
 
 extern "C" int gl_debug_inject_alloc_failures(int count) {
@@ -1104,18 +1186,36 @@ extern "C" int gl_debug_inject_alloc_failures(int count) {
   return GL_OK;
 }
 
-void gl_init_mempool_once() {
-  static std::once_flag once;
-  std::call_once(once, [] {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return;
-    cudaMemPool_t pool;
-    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-      uint64_t keep = UINT64_MAX;  // keep freed blocks cached in this process
-      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-    }
-  });
+// The library's stream-ordered memory pool on the current device (one per
+// device, created on first use).  Freed blocks stay cached in the process,
+// and an allocation never reuses a block whose free is still pending on
+// another stream: with the default pool's internal dependencies a small
+// request's scratch could wait for a long request on another stream to free
+// its memory.  Blocks whose free has completed are reused (opportunistic
+// reuse); otherwise the pool grows.
+cudaMemPool_t gl_mempool() {
+  static std::mutex mu;
+  static std::map<int, cudaMemPool_t> pools;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = pools.find(dev);
+  if (it != pools.end()) return it->second;
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool = nullptr;
+  if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) return nullptr;
+  uint64_t keep = UINT64_MAX;
+  cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  int off = 0;
+  cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &off);
+  pools.emplace(dev, pool);
+  return pool;
 }
+
+void gl_init_mempool_once() { gl_mempool(); }
 
 // Device address of host memory [p, p + bytes) that kernels can read and
 // write in place: page-locked memory mapped into the device address space
@@ -1320,8 +1420,9 @@ static int coset_tables(uint64_t g, uint64_t n, const uint64_t **lo, const uint6
     int st = upload(holder, mont_powers(g, GL_TW_SPLIT, 1), &a);
     if (st == GL_OK)
       st = upload(holder, mont_powers(gl_pow(g, GL_TW_SPLIT), (n + GL_TW_SPLIT - 1) / GL_TW_SPLIT, 1), &b);
+    if (st == GL_OK) st = gl_table_sync();
     if (st != GL_OK) {
-      for (void *p : holder.owned) cudaFree(p);
+      gl_table_free(holder.owned);
       return st;
     }
     it = g_coset.emplace(key, std::make_pair(a, b)).first;

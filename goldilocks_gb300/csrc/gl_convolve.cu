@@ -85,3 +85,5 @@ extern "C" int gl_convolve(uint64_t *a, const uint64_t *b_hat, uint64_t n, uint6
   if (e != cudaSuccess) return gl_cuda_status(e);
   return gl_cuda_status(e2);
 }
+
+void gl_convolve_kernels(std::vector<const void *> &out) { out.push_back((const void *)gl_pointwise_kernel); }

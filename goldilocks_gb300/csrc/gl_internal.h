@@ -27,6 +27,9 @@ struct gl_nvtx_range {
 // injected on the host (gl_debug_inject_alloc_failures) to test that
 // GL_ERR_OOM propagates without touching the caller's data.  (gl_api.cu)
 cudaError_t gl_malloc_async(void **p, size_t bytes, cudaStream_t stream);
+// The library's memory pool on the current device (no cross-stream reuse
+// dependencies; freed blocks kept).  (gl_api.cu)
+cudaMemPool_t gl_mempool();
 
 typedef void (*gl_launch_fn)(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
 
@@ -40,6 +43,7 @@ struct gl_kernel_entry {
   int threads;
   gl_launch_fn launch;
   bool generic = false;  // gl_generic_kernel: radices passed at run time
+  const void *func = nullptr;  // the __global__ function (gl_preload_kernels)
 };
 
 // Kernel sets compiled in separate translation units (parallel build).
@@ -61,6 +65,13 @@ const gl_kernel_entry *gl_kernels_pass2_inv(size_t *count);
 // Run-time-radix kernels (gl_kern_generic.cu).
 void gl_launch_generic_fwd(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
 void gl_launch_generic_inv(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
+const void *gl_generic_kernel_fwd();
+const void *gl_generic_kernel_inv();
+// The other __global__ functions of the batch, Rader and convolution paths,
+// for gl_preload_kernels (gl_batch.cu, gl_rader.cu, gl_convolve.cu).
+void gl_batch_kernels(std::vector<const void *> &out);
+void gl_rader_kernels(std::vector<const void *> &out);
+void gl_convolve_kernels(std::vector<const void *> &out);
 #include "gl_generic.cuh"
 
 // Opt in to more than 48 KB of dynamic shared memory once per kernel and
@@ -136,8 +147,16 @@ struct gl_plan {
   std::map<int, gl_dev_tables> dev;  // per device id
 };
 
-// Twiddle tables of `pl` on the current device (built on first use).
+// Twiddle tables of `pl` on the current device (built on first use, on the
+// table stream: no device-wide synchronisation).
 int gl_plan_tables(gl_plan *pl, gl_dev_tables **out);
+// The library's table stream of the current device; a stream-ordered upload
+// of `bytes` from host memory into a new table owned by `t` (complete after
+// gl_table_sync); freeing the tables of a plan.  (gl_api.cu)
+cudaStream_t gl_table_stream();
+int gl_table_upload(gl_dev_tables &t, const void *h, size_t bytes, void **dst);
+int gl_table_sync();
+void gl_table_free(std::vector<void *> &owned);
 // Launch `k` (optionally bracketed by profiling events).  role: 0 full,
 // 1 col, 2 row.
 void gl_launch(const gl_kernel_entry *k, int role, const gl_pass_args &a, dim3 grid,

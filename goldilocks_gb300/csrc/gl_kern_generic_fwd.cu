@@ -4,3 +4,5 @@
 void gl_launch_generic_fwd(const gl_pass_args &args, dim3 grid, cudaStream_t stream) {
   gl_launch_generic<false>(args, grid, stream);
 }
+
+const void *gl_generic_kernel_fwd() { return (const void *)gl_generic_kernel<false>; }

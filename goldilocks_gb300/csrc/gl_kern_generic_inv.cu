@@ -4,3 +4,5 @@
 void gl_launch_generic_inv(const gl_pass_args &args, dim3 grid, cudaStream_t stream) {
   gl_launch_generic<true>(args, grid, stream);
 }
+
+const void *gl_generic_kernel_inv() { return (const void *)gl_generic_kernel<true>; }

@@ -14,10 +14,12 @@ static void gl_launch_pass3(const gl_pass_args &args, dim3 grid, cudaStream_t st
 
 #define GL_ENTRY3(R1, R2, R3, LANES, NT, INV)                                                 \
   {R1 * R2 * R3, R1, R2, R3, LANES, INV, gl_p3_smem_bytes<R1, R2, R3, LANES>(), NT,          \
-   gl_launch_pass3<R1, R2, R3, LANES, NT, INV>}
+   gl_launch_pass3<R1, R2, R3, LANES, NT, INV>, false,                                        \
+   (const void *)gl_pass3_kernel<R1, R2, R3, LANES, NT, INV, 1>}
 
 // MINB CTAs resident per SM (registers capped to fit), so that one CTA's
 // loads overlap another's arithmetic.
 #define GL_ENTRY3M(R1, R2, R3, LANES, NT, MINB, INV)                                          \
   {R1 * R2 * R3, R1, R2, R3, LANES, INV, gl_p3_smem_bytes<R1, R2, R3, LANES>(), NT,          \
-   gl_launch_pass3<R1, R2, R3, LANES, NT, INV, MINB>}
+   gl_launch_pass3<R1, R2, R3, LANES, NT, INV, MINB>, false,                                  \
+   (const void *)gl_pass3_kernel<R1, R2, R3, LANES, NT, INV, MINB>}

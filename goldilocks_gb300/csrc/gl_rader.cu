@@ -40,14 +40,7 @@ unsigned grid_for(uint64_t items) {
 
 template <typename T>
 int upload(gl_dev_tables &t, const std::vector<T> &h, T **dst) {
-  void *p = nullptr;
-  cudaError_t e = cudaMalloc(&p, h.size() * sizeof(T));
-  if (e != cudaSuccess) return gl_cuda_status(e);
-  e = cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) { cudaFree(p); return gl_cuda_status(e); }
-  t.owned.push_back(p);
-  *dst = (T *)p;
-  return GL_OK;
+  return gl_table_upload(t, h.data(), h.size() * sizeof(T), (void **)dst);
 }
 
 }  // namespace
@@ -158,18 +151,14 @@ int gl_rader_tables(gl_plan *pl, gl_dev_tables &t) {
     for (uint64_t s = 0; s < r; s++) bv[s] = gl_pow(wq, gn[s]);
     if (st == GL_OK) st = upload(t, bv, &t.rader_bhat[d]);
     if (st != GL_OK) break;
-    cudaStream_t s0;
-    cudaError_t e = cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking);
-    if (e != cudaSuccess) return gl_cuda_status(e);
+    // Transformed on the table stream, after its upload there; the caller
+    // (gl_plan_tables) synchronises that stream before the tables are used.
+    cudaStream_t ts = gl_table_stream();
     uint64_t *scr = nullptr;
     const uint64_t sw = gl_plan_scratch_words(pl->pq, 1, 1);
-    if (sw) e = cudaMalloc((void **)&scr, sw * sizeof(uint64_t));
-    if (e == cudaSuccess) {
-      st = gl_enqueue_transform(pl->pq, t.rader_bhat[d], t.rader_bhat[d], 1, 1, r, false, scr, s0);
-      e = cudaStreamSynchronize(s0);
-    }
-    if (scr) cudaFree(scr);
-    cudaStreamDestroy(s0);
+    cudaError_t e = sw ? gl_malloc_async((void **)&scr, sw * sizeof(uint64_t), ts) : cudaSuccess;
+    if (e == cudaSuccess) st = gl_enqueue_transform(pl->pq, t.rader_bhat[d], t.rader_bhat[d], 1, 1, r, false, scr, ts);
+    if (scr) cudaFreeAsync(scr, ts);
     if (st == GL_OK && e != cudaSuccess) st = gl_cuda_status(e);
   }
   return st;
@@ -216,4 +205,11 @@ int gl_rader_enqueue(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64_t C
       return st;
   }
   return GL_OK;
+}
+
+void gl_rader_kernels(std::vector<const void *> &out) {
+  out.push_back((const void *)gl_rader_gather_kernel);
+  out.push_back((const void *)gl_rader_pointwise_kernel);
+  out.push_back((const void *)gl_rader_scatter_kernel);
+  out.push_back((const void *)gl_rader_scatter_tiled_kernel);
 }

@@ -279,6 +279,11 @@ extern "C" int gl_server_create(uint64_t budget_bytes, int slots, int max_batch,
   cudaError_t e = cudaGetDevice(&s->device);
   if (e != cudaSuccess) { delete s; return gl_cuda_status(e); }
   gl_init_mempool_once();
+  // Every kernel loaded now, while the device is idle: under lazy loading the
+  // first launch of a kernel would wait for the requests running on the other
+  // slots.
+  const int pst = gl_preload_kernels();
+  if (pst != GL_OK) { delete s; return pst; }
   s->slots.resize(slots);
   int prio_low = 0, prio_high = 0;
   cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);

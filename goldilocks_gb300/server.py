@@ -114,6 +114,13 @@ def _out_words(op, n, cols, blowup):
     return n * cols * (blowup if op == GL_OP_LDE else 1)
 
 
+SMALL_WORDS = 1 << 21  # the server's small-request class: at most this many output words
+
+
+def _is_small(req):
+    return _out_words(*req) <= SMALL_WORDS
+
+
 def _buffers(torch, reqs, pool):
     """Per request: input = a slice of a resident pool, output = its own buffer."""
     outs, ins = [], []
@@ -164,11 +171,17 @@ def serve_stream(reqs, arrivals, pool, budget_bytes=64 << 30, slots=4, max_batch
     completion (`latency_ms`, and p50/p99 of it).  With ring_words > 0 the
     outputs share a ring of that many words: each returned output is a view of
     the ring, which a later request may have overwritten -- except the
-    requests whose indices are in `keep`, which get buffers of their own."""
+    requests whose indices are in `keep`, which get buffers of their own.
+    Small requests (the server's class) take their outputs from a ring of
+    their own (a sixteenth of ring_words, at least 2^22 words, at most half),
+    so that the submitter never holds a small request back until a large one
+    has finished."""
     import torch
     keep = set(keep)
     if ring_words:
-        ins, outs, ring = [pool[:n * c] for _, n, c, _ in reqs], [], _Ring(torch, ring_words)
+        small_words = min(ring_words // 2, max(ring_words // 16, 1 << 22))
+        ins, outs = [pool[:n * c] for _, n, c, _ in reqs], []
+        ring = {True: _Ring(torch, small_words), False: _Ring(torch, ring_words - small_words)}
         own = {k: torch.empty(_out_words(*reqs[k]), dtype=torch.int64, device="cuda") for k in sorted(keep)}
     else:
         (ins, outs), ring, own = _buffers(torch, reqs, pool), None, {}
@@ -187,11 +200,12 @@ def serve_stream(reqs, arrivals, pool, budget_bytes=64 << 30, slots=4, max_batch
             now = time.perf_counter() - t0
             if a > now:
                 time.sleep(a - now)
+            small = _is_small(reqs[k])
             if k in own:
                 o = own[k]
                 outs.append(o)
             elif ring:
-                o, lo, hi = ring.take(_out_words(op, n, cols, blowup), wait)
+                o, lo, hi = ring[small].take(_out_words(op, n, cols, blowup), wait)
                 outs.append(o)
             else:
                 o = outs[k]
@@ -199,7 +213,7 @@ def serve_stream(reqs, arrivals, pool, budget_bytes=64 << 30, slots=4, max_batch
             rid = srv.submit(op, n, cols, i, o, blowup)
             pending[rid] = (k, max(t_sub, float(a)))
             if ring and k not in own:
-                ring.live.append((rid, lo, hi))
+                ring[small].live.append((rid, lo, hi))
         for rid in list(pending):
             wait(rid)
         wall = time.perf_counter() - t0
@@ -326,7 +340,7 @@ def compare_at_loads(reqs, pool, loads, seed, budget_bytes=64 << 30, slots=4, ma
     p99 at the same load."""
     ser_rate, ser_lat, ser_wall, _ = serial_baseline(reqs, pool, ring_words=ring_words or 1)
     elements = sum(n * c for _, n, c, _ in reqs)
-    small = [k for k, r in enumerate(reqs) if _out_words(*r) <= 1 << 21]
+    small = [k for k, r in enumerate(reqs) if _is_small(r)]
     res = {"requests": len(reqs), "elements": elements,
            "serial": {"elem_s": ser_rate, "wall_s": ser_wall, "service_p50_ms": ser_lat["p50_ms"],
                       "service_p99_ms": ser_lat["p99_ms"]},

@@ -316,6 +316,28 @@ typedef struct {
 
 typedef struct gl_server gl_server;
 
+/* ---- standalone permutations (ntt/src/permute/mod.rs) ---- */
+
+/* In-place transpose of the row-major rows x cols matrix `data` of words:
+ * afterwards data[i * rows + j] holds the former data[j * cols + i] (a
+ * cols x rows matrix).  Replaces permute::transpose (ntt/src/permute/mod.rs:
+ * 53-58; the same result as transpose_copy, mod.rs:60-68).  Host memory:
+ * copied in and out, synchronously; device memory: queued on `stream`
+ * (scratch of rows * cols words from the library's pool). */
+int gl_transpose(uint64_t *data, uint64_t rows, uint64_t cols, int mem, void *stream);
+/* In-place bit-reversal permutation of n words (n a power of two, else
+ * GL_ERR_UNSUPPORTED_SIZE where the reference asserts): data[i] and
+ * data[rev(i)] exchanged.  Replaces permute::bit_reverse
+ * (ntt/src/permute/mod.rs:70-74, permutation.rs:11-15). */
+int gl_bit_reverse(uint64_t *data, uint64_t n, int mem, void *stream);
+
+/* Load every kernel of the library onto the current device now (no
+ * counterpart in the reference).  Under CUDA's lazy module loading a kernel
+ * is loaded at its first launch, and that load waits for the work already
+ * running on the device; a multi-stream caller that must not stall calls
+ * this during set-up.  gl_server_create calls it. */
+int gl_preload_kernels(void);
+
 /* A server on the current device with `slots` concurrent batches (one CUDA
  * stream each), at most `max_batch` requests per batch, and `budget_bytes` of
  * device memory for the temporaries of requests in flight.  With two slots or
