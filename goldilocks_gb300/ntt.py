@@ -180,6 +180,28 @@ def host_pipeline(jobs, depth=0):
     return [a for a, _, _ in jobs]
 
 
+def transpose(values, shape):
+    """permute::transpose (ntt/src/permute/mod.rs:53-58): the row-major
+    rows x cols matrix `values` transposed in place (it becomes cols x rows)."""
+    rows, cols = shape
+    ptr, n, mem, stream = _buffer(values)
+    if n != rows * cols:
+        raise ValueError("matrix of %d values is not %d x %d" % (n, rows, cols))
+    _check(L.load().gl_transpose(ptr, rows, cols, mem, stream), "transpose")
+    return values
+
+
+def bit_reverse(values):
+    """permute::bit_reverse (ntt/src/permute/mod.rs:70-74): values[i] and
+    values[rev(i)] exchanged, for a power-of-two length."""
+    ptr, n, mem, stream = _buffer(values)
+    st = L.load().gl_bit_reverse(ptr, n, mem, stream)
+    if st == L.GL_ERR_UNSUPPORTED_SIZE:
+        raise ValueError("bit_reverse needs a power-of-two length, got %d" % n)
+    _check(st, "bit_reverse")
+    return values
+
+
 def clear_cache():
     L.load().gl_clear_cache()
 
