@@ -131,19 +131,35 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def ncu_per_element(name):
-    """Per-element figures of each kernel from the committed ncu summary:
-    ncu_traffic.json (DRAM bytes read + written), ncu_inst.json (thread
-    instructions executed)."""
+# Sources whose change invalidates the committed ncu figures of the pass kernels.
+KERNEL_SOURCES = ("gl_pass3.cuh", "gl_pass.cuh", "gl_field.cuh", "gl_codelets.cuh", "gl_kernels_impl.cuh",
+                  "gl_kern_pass_fwd.cu", "gl_kern_pass_inv.cu", "gl_kern_mixed17_fwd.cu", "gl_kern_mixed17_inv.cu")
+
+
+def kernel_source_sha():
+    """sha256 (first 16 hex digits) of the pass-kernel sources, in a fixed order."""
+    import hashlib
+    h = hashlib.sha256()
+    for name in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, "goldilocks_gb300", "csrc", name), "rb") as f:
+            h.update(name.encode() + b"\0" + f.read())
+    return h.hexdigest()[:16]
+
+
+def ncu_per_element():
+    """Per-element figures of each pass kernel from the committed ncu capture
+    (profiles/ncu_pass_kernels.json: DRAM bytes read + written and thread
+    instructions executed per element), or ({}, reason) when the file is
+    missing or was measured on other kernel sources than these."""
     try:
-        with open(os.path.join(ROOT, "profiles", name)) as f:
-            return json.load(f)
-    except Exception:
-        return {}
-
-
-def ncu_traffic():
-    return ncu_per_element("ncu_traffic.json")
+        with open(os.path.join(ROOT, "profiles", "ncu_pass_kernels.json")) as f:
+            d = json.load(f)
+    except Exception as e:
+        return {}, "no committed ncu figures (%s)" % type(e).__name__
+    if d.get("source_sha") != kernel_source_sha():
+        return {}, "committed ncu figures are for other kernel sources (sha %s, now %s)" % (
+            d.get("source_sha"), kernel_source_sha())
+    return d.get("kernels", {}), None
 
 
 def host_cpu():
@@ -564,10 +580,13 @@ def run_ours(args):
         per_launch_el = dom["elements"] / dom["launches"]
         mean_ms = dom["total_ms"] / dom["launches"]
         achieved = 16.0 * per_launch_el / (mean_ms * 1e-3) / 1e9
-        tr = ncu_traffic().get(dom["name"])
+        figs, stale = ncu_per_element()
+        tr = figs.get(dom["name"], {}).get("dram_bytes_per_element")
         roofline = {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": peak,
                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                     "traffic": (tr * per_launch_el) if tr else None,
+                    "traffic_basis": stale or "ncu DRAM bytes per element of this kernel (committed capture of "
+                                              "these sources, profiles/ncu_pass_kernels.json) x elements per launch",
                     "algorithmic_bytes_per_launch": 16.0 * per_launch_el,
                     "mean_launch_ms": mean_ms,
                     "share": dom["total_ms"] / max(sum(p["total_ms"] for p in prof), 1e-12)}
@@ -575,7 +594,7 @@ def run_ours(args):
     # instructions per SM per clock), from the ncu instruction count per
     # element and the live launch time, at the SM clock sampled during the run.
     issue = None
-    inst = ncu_per_element("ncu_inst.json").get(dom["name"]) if dom else None
+    inst = ncu_per_element()[0].get(dom["name"], {}).get("inst_per_element") if dom else None
     if inst and clk and clk.get("sm_mhz"):
         sms = torch.cuda.get_device_properties(local).multi_processor_count
         per_launch_el = dom["elements"] / dom["launches"]
@@ -585,8 +604,8 @@ def run_ours(args):
         issue = {"bound": "integer issue", "kernel": dom["name"], "inst_per_element": inst,
                  "achieved": achieved_i, "peak": peak_i, "unit": "G warp-instructions/s",
                  "frac": achieved_i / peak_i,
-                 "basis": "thread instructions per element from the committed ncu capture; "
-                          "4 warp instructions per SM per clock at the sampled SM clock"}
+                 "basis": "thread instructions per element from the committed ncu capture of these "
+                          "kernel sources; 4 warp instructions per SM per clock at the sampled SM clock"}
     # whole-transform roofline: 16 B * n * passes(n) per transform, passes = ceil(log2 n / 14)
     import math
     alg_bytes = sum(2 * 16 * n * math.ceil(math.log2(n) / 14) for n in SIZES)
