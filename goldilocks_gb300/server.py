@@ -172,50 +172,76 @@ def serve_stream(reqs, arrivals, pool, budget_bytes=64 << 30, slots=4, max_batch
     outputs share a ring of that many words: each returned output is a view of
     the ring, which a later request may have overwritten -- except the
     requests whose indices are in `keep`, which get buffers of their own.
-    Small requests (the server's class) take their outputs from a ring of
-    their own (a sixteenth of ring_words, at least 2^22 words, at most half),
-    so that the submitter never holds a small request back until a large one
-    has finished."""
+    Small and large requests (the server's classes) are submitted by two
+    client threads, each with an output ring of its own (the small one a
+    sixteenth of ring_words, at least 2^22 words, at most half), so that a
+    client waiting for ring space never delays the other class's
+    submissions."""
+    import threading
+
     import torch
     keep = set(keep)
+    classes = {True: [k for k in range(len(reqs)) if _is_small(reqs[k])],
+               False: [k for k in range(len(reqs)) if not _is_small(reqs[k])]}
+    ins = [pool[:n * c] for _, n, c, _ in reqs]
     if ring_words:
         small_words = min(ring_words // 2, max(ring_words // 16, 1 << 22))
-        ins, outs = [pool[:n * c] for _, n, c, _ in reqs], []
         ring = {True: _Ring(torch, small_words), False: _Ring(torch, ring_words - small_words)}
         own = {k: torch.empty(_out_words(*reqs[k]), dtype=torch.int64, device="cuda") for k in sorted(keep)}
     else:
-        (ins, outs), ring, own = _buffers(torch, reqs, pool), None, {}
+        ring, own = None, {}
+        _, outs_all = _buffers(torch, reqs, pool)
+        own = dict(enumerate(outs_all))
     torch.cuda.synchronize()
-    pending = collections.OrderedDict()  # rid -> (request index, submit time)
+    outs = [None] * len(reqs)
     lat = [0.0] * len(reqs)
+    sub = [None] * len(reqs)  # (rid, submit time) per request
+    lock = threading.Lock()
+    waited = set()
+    errors = []
     with Server(budget_bytes, slots, max_batch) as srv:
-        def wait(rid):
-            k, t_sub = pending.pop(rid)
+        def wait(k):
+            with lock:
+                if k in waited:
+                    return
+                waited.add(k)
+            rid, t_sub = sub[k]
             st, ms = srv.wait_timed(rid, timeout_ms=600000)
             if st != L.GL_OK:
                 raise GoldilocksError(st, "request")
             lat[k] = (t_sub - arrivals[k]) * 1e3 + ms  # from arrival, not from submission
+
+        def client(small):
+            try:
+                r = ring[small] if ring else None
+                for k in classes[small]:
+                    op, n, cols, blowup = reqs[k]
+                    now = time.perf_counter() - t0
+                    if arrivals[k] > now:
+                        time.sleep(arrivals[k] - now)
+                    if k in own:
+                        o = own[k]
+                    else:
+                        o, lo, hi = r.take(_out_words(op, n, cols, blowup), wait)
+                    outs[k] = o
+                    t_sub = time.perf_counter() - t0
+                    rid = srv.submit(op, n, cols, ins[k], o, blowup)
+                    sub[k] = (rid, max(t_sub, float(arrivals[k])))
+                    if r is not None and k not in own:
+                        r.live.append((k, lo, hi))
+            except Exception as e:  # reported by the caller
+                errors.append(e)
+
         t0 = time.perf_counter()
-        for k, ((op, n, cols, blowup), a, i) in enumerate(zip(reqs, arrivals, ins)):
-            now = time.perf_counter() - t0
-            if a > now:
-                time.sleep(a - now)
-            small = _is_small(reqs[k])
-            if k in own:
-                o = own[k]
-                outs.append(o)
-            elif ring:
-                o, lo, hi = ring[small].take(_out_words(op, n, cols, blowup), wait)
-                outs.append(o)
-            else:
-                o = outs[k]
-            t_sub = time.perf_counter() - t0
-            rid = srv.submit(op, n, cols, i, o, blowup)
-            pending[rid] = (k, max(t_sub, float(a)))
-            if ring and k not in own:
-                ring[small].live.append((rid, lo, hi))
-        for rid in list(pending):
-            wait(rid)
+        threads = [threading.Thread(target=client, args=(c,)) for c in (True, False)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        if errors:
+            raise errors[0]
+        for k in range(len(reqs)):
+            wait(k)
         wall = time.perf_counter() - t0
         stats = srv.stats()
     stats["latency_ms"] = lat
