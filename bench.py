@@ -267,6 +267,11 @@ def bench_batched(gl, torch, reps=3):
         b.synchronize()
         out[name + "_elem_s"] = out["elements"] * reps / (a.elapsed_time(b) * 1e-3)
     out["persistent_vs_per_call"] = out["persistent_elem_s"] / out["per_call_elem_s"]
+    # Roofline of the batch: sum of B(n_i) = 16 n_i P(n_i) bytes over the batch's
+    # time, against the measured HBM copy bandwidth.
+    import math
+    peak, peak_kind = peaks()
+    out["algorithmic_bytes"] = alg = sum(16 * n * math.ceil(math.log2(n) / 14) for n in sizes)
     # The same batch through run_packed: (offset, length, direction) arrays
     # over the pool, so the host builds the descriptor array in one numpy
     # step instead of one Python call per polynomial.
@@ -282,6 +287,10 @@ def bench_batched(gl, torch, reps=3):
         b.record(stream)
         b.synchronize()
         out[name + "_elem_s"] = out["elements"] * reps / (a.elapsed_time(b) * 1e-3)
+    for name in ("buckets_packed", "persistent_packed", "buckets", "persistent"):
+        t = out["elements"] / out[name + "_elem_s"]
+        out[name + "_frac"] = alg / t / 1e9 / peak
+    out["peak_gbs"], out["peak_kind"] = peak, peak_kind
     # The schedules of the batch's lengths measured first (gl_plan_autotune),
     # then buckets again, and AUTO with the mode gl_batch_autotune measured.
     from goldilocks_gb300 import tune
@@ -363,9 +372,11 @@ def bench_commit(gl, torch, reps=3):
     merkle_ms = _time_ms(torch, merkle, reps)
     import math
     alg = cols * sum(16 * m * math.ceil(math.log2(m) / 14) for m in (n, n * blowup))
+    peak, peak_kind = peaks()
     res = {"shape": "2^20 x 256 -> 2^22 x 256, blowup 4, shift 7",
            "lde_ms": lde_ms, "lde_rows_cols_per_s": n * cols / (lde_ms * 1e-3),
            "lde_algorithmic_gbs": alg / (lde_ms * 1e-3) / 1e9,
+           "lde_frac": alg / (lde_ms * 1e-3) / 1e9 / peak, "peak_gbs": peak, "peak_kind": peak_kind,
            "merkle_ms": merkle_ms, "merkle_leaf_bytes": leaves,
            "merkle_leaf_gbs": leaves / (merkle_ms * 1e-3) / 1e9,
            "merkle_permutations_per_s": (leaves + tree_bytes) / 160 / (merkle_ms * 1e-3),

@@ -310,12 +310,13 @@ def serial_fifo(service_ms, arrivals):
 
 def check_sample(reqs, count, seed, max_words):
     """Indices of requests whose served outputs are kept and checked: the
-    largest request of each operation, then a seeded sample, while the kept
-    outputs total at most max_words."""
+    largest request of each operation whose output is at most a quarter of
+    max_words, then a seeded sample, while the kept outputs total at most
+    max_words."""
     rng = np.random.default_rng(seed)
     order = []
     for op in (GL_OP_LDE, GL_OP_NTT, GL_OP_INTT):
-        ks = [k for k, r in enumerate(reqs) if r[0] == op]
+        ks = [k for k, r in enumerate(reqs) if r[0] == op and _out_words(*r) <= max_words // 4]
         if ks:
             order.append(max(ks, key=lambda k: _out_words(*reqs[k])))
     order += [int(k) for k in rng.permutation(len(reqs))]
