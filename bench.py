@@ -29,6 +29,7 @@ reference is Rust and no Rust toolchain exists here) on all usable host
 threads, for the same metric and workload.
 """
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -503,6 +504,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
+    gc.collect()
+    gc.disable()  # no collector pauses between the timed launches (see timed() below)
     for _ in range(args.steps):
         flush.zero_()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -511,6 +514,7 @@ def run_ours(args):
         b.record(stream)
         evs.append((a, b))
     torch.cuda.synchronize()
+    gc.enable()
     if dist:
         dist.barrier()
     clk = clocks.stop()
@@ -554,17 +558,25 @@ def run_ours(args):
         # Two untimed calls, then e2e_steps timed ones (each synchronous);
         # the value is the total over the timed steps, and every step's time
         # is reported beside it so that an outlier is visible.
+        # Python's garbage collector is paused inside the timed loop (as timeit
+        # does): a full collection of this process's objects takes 10-20 ms,
+        # host time that is not part of the work measured.
         fn()
         fn()
         if dist:
             dist.barrier()
         times = []
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            t = time.perf_counter()
-            fn()
-            times.append((time.perf_counter() - t) * 1e3)
-        total = time.perf_counter() - t0
+        gc.collect()
+        gc.disable()
+        try:
+            t0 = time.perf_counter()
+            for _ in range(e2e_steps):
+                t = time.perf_counter()
+                fn()
+                times.append((time.perf_counter() - t) * 1e3)
+            total = time.perf_counter() - t0
+        finally:
+            gc.enable()
         step_ms[name] = [round(x, 3) for x in times]
         return max_over_ranks(dist, total, "cuda")
     e2e_s = timed(host_step, "pipeline")
