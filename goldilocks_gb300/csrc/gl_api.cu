@@ -219,7 +219,8 @@ extern "C" int gl_preload_kernels(void) {
   GL_NVTX("gl_preload_kernels");
   std::vector<const void *> funcs;
   using table_fn = const gl_kernel_entry *(*)(size_t *);
-  for (table_fn f : {gl_kernels_full_fwd, gl_kernels_full_inv, gl_kernels_pass_fwd, gl_kernels_pass_inv,
+  for (table_fn f : {gl_kernels_full_fwd, gl_kernels_full_inv, gl_kernels_full1_fwd, gl_kernels_full1_inv,
+                     gl_kernels_pass_fwd, gl_kernels_pass_inv,
                      gl_kernels_mixed35_fwd, gl_kernels_mixed35_inv, gl_kernels_mixed17_fwd,
                      gl_kernels_mixed17_inv, gl_kernels_pass2_fwd, gl_kernels_pass2_inv, gl_kernels_cols_fwd,
                      gl_kernels_cols_inv}) {
@@ -250,6 +251,20 @@ static std::string kernel_shape(const gl_kernel_entry *k) {
 }
 
 // ------------------------------------------------------------------- plans
+
+// Multiprocessors of the current device (cached per device).
+int gl_sm_count() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 1;
+  if (dev < 64) {
+    if (int v = cache[dev].load(std::memory_order_relaxed)) return v;
+  }
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) return 1;
+  if (dev < 64) cache[dev].store(sms, std::memory_order_relaxed);
+  return sms;
+}
 
 static std::mutex g_cache_mu;
 static std::map<uint64_t, gl_plan *> g_cache;
@@ -438,7 +453,12 @@ bool gl_choice_apply(gl_plan *pl, const gl_choice &c) {
   pl->n3 = c.n3;
   const uint64_t f[3] = {c.n1, c.n2, c.n3};
   for (int d = 0; d < 2; d++) {
-    if (c.kind == 1) pl->k[0][d] = gl_find_kernel(n, true, d == 1);
+    if (c.kind == 1) {
+      pl->k[0][d] = gl_find_kernel(n, true, d == 1);
+      size_t cnt = 0;
+      const gl_kernel_entry *e = d == 1 ? gl_kernels_full1_inv(&cnt) : gl_kernels_full1_fwd(&cnt);
+      pl->k1[d] = find_in(e, cnt, n);
+    }
     for (int s = 0; c.kind >= 2 && s < c.kind; s++) {
       pl->k[s][d] = c.lanes4 ? gl_find_kernel4(f[s], d == 1) : gl_find_kernel(f[s], false, d == 1);
       pl->k4[s][d] = gl_find_kernel_cols(f[s], d == 1);
@@ -796,12 +816,12 @@ static std::vector<gl_prof_rec> g_prof;
 
 static std::string kernel_label(const gl_kernel_entry *k, int role) {
   static const char *roles[] = {"full", "col", "row"};
-  return std::string(roles[role]) + " " + kernel_shape(k);
+  return std::string(roles[role]) + " " + kernel_shape(k) + (role == 0 && k->lanes == 1 ? " single" : "");
 }
 
 // Launch `k` with optional event bracketing.  role: 0 full, 1 col, 2 row.
 void gl_launch(const gl_kernel_entry *k, int role, const gl_pass_args &a0, dim3 grid,
-                   uint64_t elements, cudaStream_t stream) {
+               uint64_t elements, cudaStream_t stream, bool pdl) {
   gl_pass_args a = a0;
   if (k->generic) { a.gen_r[0] = k->r1; a.gen_r[1] = k->r2; a.gen_r[2] = k->r3; }
   bool on;
@@ -811,12 +831,12 @@ void gl_launch(const gl_kernel_entry *k, int role, const gl_pass_args &a0, dim3 
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   if (on && cudaStreamIsCapturing(stream, &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone)
     on = false;
-  if (!on) { k->launch(a, grid, stream); return; }
+  if (!on) { k->launch(a, grid, stream, pdl); return; }
   gl_prof_rec r{k, role, elements, nullptr, nullptr};
   cudaEventCreate(&r.a);
   cudaEventCreate(&r.b);
   cudaEventRecord(r.a, stream);
-  k->launch(a, grid, stream);
+  k->launch(a, grid, stream, false);
   cudaEventRecord(r.b, stream);
   std::lock_guard<std::mutex> lk(g_prof_mu);
   g_prof.push_back(r);
@@ -940,6 +960,8 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
   };
   if (pl->kind == 1) {
     const gl_kernel_entry *k = pl->k[0][d];
+    // Too few transforms to give every SM a CTA: one transform per CTA.
+    if (C == 1 && pl->k1[d] && (B + k->lanes - 1) / k->lanes < (uint64_t)gl_sm_count()) k = pl->k1[d];
     gl_pass_args a = base_args();
     a.tw_m = inv ? t->blk_scaled_inv : t->blk[0][0];
     a.tw_r2 = t->blk[0][d];
@@ -984,6 +1006,8 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
   if (pl->kind == 3) {
     // Three passes, n = n1*n2*n3, j = n2 n3 j1 + n3 j2 + j3,
     // k = k1 + n1 k2 + n1 n2 k3:
+    // Every pass after the first of the call is launched for programmatic
+    // dependent launch: its predecessor in the stream is a pass of this call.
     //   A  n1-point over j1, times omega_n^(j23 k1)           src -> scratch
     //   B  per k1: n2-point over j2, times omega_(n2 n3)^(j3 k2)  in place
     //   C  per (k1, k2): n3-point over j3, stored at k         scratch -> dst
@@ -1010,7 +1034,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       GL_DBG_EXTENTS(a, n * C, n * C);
       const uint64_t ta = gl_tiles(n23 * C, ka);
       if (ta > 0x7fffffffull) return GL_ERR_INVALID;
-      gl_launch(ka, 1, a, dim3((unsigned)ta), n * C, stream);
+      gl_launch(ka, 1, a, dim3((unsigned)ta), n * C, stream, b > 0);
       gl_pass_args bb = base_args();
       bb.in_limit = 0xffffffffu;
       bb.in = s1; bb.out = s1;
@@ -1022,7 +1046,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       bb.tw_lane_div = (uint32_t)C;
       GL_DBG_EXTENTS(bb, n * C, n * C);
       gl_launch(kb, 1, bb, dim3((unsigned)gl_tiles(n3 * C, kb), (unsigned)n1),
-                n * C, stream);
+                n * C, stream, true);
       gl_pass_args c = base_args();
       c.in_limit = 0xffffffffu;
       c.tw_m = c.tw_r2 = t->blk3[d];
@@ -1039,7 +1063,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
           c.mul = om->factors + b * mul_item;
           c.mul_ls = c.out_ls; c.mul_bs = c.out_bs;
         }
-        gl_launch(kcr, 2, c, dim3((unsigned)gl_tiles(n2, kcr), (unsigned)n1), n, stream);
+        gl_launch(kcr, 2, c, dim3((unsigned)gl_tiles(n2, kcr), (unsigned)n1), n, stream, true);
       } else {
         c.in_ls = 1; c.in_is = (int64_t)C;                        // lanes: columns
         c.out_ls = 1; c.out_is = (int64_t)(n1 * n2 * C);
@@ -1048,12 +1072,13 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
         c.flags |= GL_PF_LOAD_LANE_FAST;
         c.lanes = (uint32_t)C;
         gl_launch(kcr, 2, c, dim3((unsigned)gl_tiles(C, kcr), (unsigned)n2,
-                                  (unsigned)n1), n * C, stream);
+                                  (unsigned)n1), n * C, stream, true);
       }
     }
     return gl_cuda_status(cudaGetLastError());
   }
-  // Four-step: n = n1*n2, j = n2*j1 + j2, k = k1 + n1*k2.
+  // Four-step: n = n1*n2, j = n2*j1 + j2, k = k1 + n1*k2.  Every pass after
+  // the first of the call is launched for programmatic dependent launch.
   const uint64_t n1 = pl->n1, n2 = pl->n2;
   const auto &ks = C > 1 ? pl->k4 : pl->k;  // interleaved columns: four-lane kernels
   const gl_kernel_entry *kc = ks[0][d], *kr = ks[1][d];
@@ -1082,7 +1107,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
     const uint64_t lanes1 = n2 * C;
     if (gl_tiles(lanes1, kc) > 0x7fffffffull) return GL_ERR_INVALID;
     gl_launch(kc, 1, a, dim3((unsigned)gl_tiles(lanes1, kc), (unsigned)cb),
-           cb * n * C, stream);
+              cb * n * C, stream, off > 0);
     // ROW: n2-point transforms along j2 for every (k1, c); transposed store.
     gl_pass_args b = base_args();
     b.in_limit = 0xffffffffu;  // zero padding applies to the first pass only
@@ -1099,7 +1124,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
         b.mul = om->factors + off * mul_item;
         b.mul_ls = 1; b.mul_bs = mul_item;
       }
-      gl_launch(kr, 2, b, dim3((unsigned)gl_tiles(n1, kr), (unsigned)cb), cb * n, stream);
+      gl_launch(kr, 2, b, dim3((unsigned)gl_tiles(n1, kr), (unsigned)cb), cb * n, stream, true);
     } else {
       b.in = scratch + off * n * C; b.out = dst + off * bs;
       b.in_ls = 1; b.in_is = (int64_t)C; b.out_ls = 1; b.out_is = (int64_t)(n1 * C);
@@ -1108,7 +1133,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       b.flags |= GL_PF_LOAD_LANE_FAST;
       b.lanes = (uint32_t)C;
       gl_launch(kr, 2, b, dim3((unsigned)gl_tiles(C, kr), (unsigned)n1,
-                            (unsigned)cb), cb * n * C, stream);
+                            (unsigned)cb), cb * n * C, stream, true);
     }
   }
   return gl_cuda_status(cudaGetLastError());

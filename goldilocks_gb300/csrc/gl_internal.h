@@ -31,7 +31,10 @@ cudaError_t gl_malloc_async(void **p, size_t bytes, cudaStream_t stream);
 // dependencies; freed blocks kept).  (gl_api.cu)
 cudaMemPool_t gl_mempool();
 
-typedef void (*gl_launch_fn)(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
+// pdl: launch with programmatic stream serialization (the kernel may start
+// while the previous kernel of the stream finishes; see gl_pdl_wait).  Only
+// for a pass whose predecessor in the stream is a pass of the same call.
+typedef void (*gl_launch_fn)(const gl_pass_args &args, dim3 grid, cudaStream_t stream, bool pdl);
 
 // One compiled instance of a pass kernel: gl_pass3_kernel (radices r1 x r2 x
 // r3, up to three register rounds), or the run-time-radix gl_generic_kernel
@@ -51,6 +54,9 @@ struct gl_kernel_entry {
 // `pass`: four-step column/row passes (LANES = 4).
 const gl_kernel_entry *gl_kernels_full_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_full_inv(size_t *count);
+// `full1`: one transform per CTA (lengths 512-4096), for calls with few transforms.
+const gl_kernel_entry *gl_kernels_full1_fwd(size_t *count);
+const gl_kernel_entry *gl_kernels_full1_inv(size_t *count);
 const gl_kernel_entry *gl_kernels_pass_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_pass_inv(size_t *count);
 // Four-lane passes of mixed-radix sizes (factors 3 or 5; factor 17).
@@ -63,8 +69,8 @@ const gl_kernel_entry *gl_kernels_pass2_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_pass2_inv(size_t *count);
 
 // Run-time-radix kernels (gl_kern_generic.cu).
-void gl_launch_generic_fwd(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
-void gl_launch_generic_inv(const gl_pass_args &args, dim3 grid, cudaStream_t stream);
+void gl_launch_generic_fwd(const gl_pass_args &args, dim3 grid, cudaStream_t stream, bool pdl);
+void gl_launch_generic_inv(const gl_pass_args &args, dim3 grid, cudaStream_t stream, bool pdl);
 const void *gl_generic_kernel_fwd();
 const void *gl_generic_kernel_inv();
 // The other __global__ functions of the batch, Rader and convolution paths,
@@ -142,6 +148,8 @@ struct gl_plan {
   // CTA (a two-lane CTA would read and write 16-byte row pieces), 8-32 lanes
   // for passes up to 512 points.
   const gl_kernel_entry *k4[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+  // kind 1: the one-transform-per-CTA kernel (nullptr below 512 points).
+  const gl_kernel_entry *k1[2] = {nullptr, nullptr};
   std::string tree;
   std::mutex mu;
   std::map<int, gl_dev_tables> dev;  // per device id
@@ -158,11 +166,12 @@ int gl_table_upload(gl_dev_tables &t, const void *h, size_t bytes, void **dst);
 int gl_table_sync();
 void gl_table_free(std::vector<void *> &owned);
 // Launch `k` (optionally bracketed by profiling events).  role: 0 full,
-// 1 col, 2 row.
+// 1 col, 2 row; pdl as for gl_launch_fn.
 void gl_launch(const gl_kernel_entry *k, int role, const gl_pass_args &a, dim3 grid,
-               uint64_t elements, cudaStream_t stream);
+               uint64_t elements, cudaStream_t stream, bool pdl = false);
 int gl_cuda_status(cudaError_t e);
 void gl_init_mempool_once();
+int gl_sm_count();  // multiprocessors of the current device
 
 // Optional load-side transformation (the LDE's zero padding and coset shift).
 struct gl_load_opts {

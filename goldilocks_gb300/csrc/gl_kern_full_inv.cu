@@ -14,3 +14,18 @@ const gl_kernel_entry *gl_kernels_full_inv(size_t *count) {
   *count = sizeof(k_entries) / sizeof(k_entries[0]);
   return k_entries;
 }
+
+// One transform per CTA for lengths 512-4096 (MINB CTAs per SM at the same
+// 64 registers as the kernels above), used when a call has too few transforms
+// to give every SM a CTA of the wider kernels: a 4096-point transform alone
+// then runs 256 threads instead of a 1024-thread CTA three quarters idle
+// (three dead lanes still run the codelets).
+static const gl_kernel_entry k_single[] = {
+    GL_ENTRY3M(8, 8, 8, 1, 64, 16, true),     GL_ENTRY3M(16, 8, 8, 1, 128, 8, true),
+    GL_ENTRY3M(16, 16, 8, 1, 256, 4, true),   GL_ENTRY3M(16, 16, 16, 1, 256, 4, true),
+};
+
+const gl_kernel_entry *gl_kernels_full1_inv(size_t *count) {
+  *count = sizeof(k_single) / sizeof(k_single[0]);
+  return k_single;
+}

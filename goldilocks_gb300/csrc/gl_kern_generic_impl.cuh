@@ -4,7 +4,7 @@
 #include "gl_internal.h"
 
 template <bool INV>
-static void gl_launch_generic(const gl_pass_args &args, dim3 grid, cudaStream_t stream) {
+static void gl_launch_generic(const gl_pass_args &args, dim3 grid, cudaStream_t stream, bool) {
   const int m = args.gen_r[0] * args.gen_r[1] * args.gen_r[2];
   const size_t smem = args.gen_r[1] == 1 ? 0 : (size_t)GL_GEN_LANES * gl_gen_ls(m) * sizeof(uint64_t);
   // the opt-in is for the largest tile (m = 4096), once per device

@@ -1,8 +1,10 @@
 // Run-time-radix pass kernel, inverse direction.
 #include "gl_kern_generic_impl.cuh"
 
-void gl_launch_generic_inv(const gl_pass_args &args, dim3 grid, cudaStream_t stream) {
-  gl_launch_generic<true>(args, grid, stream);
+// Launched without programmatic dependent launch: the kernel starts once the
+// previous kernel of the stream has finished.
+void gl_launch_generic_inv(const gl_pass_args &args, dim3 grid, cudaStream_t stream, bool) {
+  gl_launch_generic<true>(args, grid, stream, false);
 }
 
 const void *gl_generic_kernel_inv() { return (const void *)gl_generic_kernel<true>; }

@@ -4,12 +4,26 @@
 #include "gl_internal.h"
 
 template <int R1, int R2, int R3, int LANES, int NT, bool INV, int MINB = 1>
-static void gl_launch_pass3(const gl_pass_args &args, dim3 grid, cudaStream_t stream) {
+static void gl_launch_pass3(const gl_pass_args &args, dim3 grid, cudaStream_t stream, bool pdl) {
   constexpr size_t smem = gl_p3_smem_bytes<R1, R2, R3, LANES>();
   auto kern = gl_pass3_kernel<R1, R2, R3, LANES, NT, INV, MINB>;
   static std::atomic<uint64_t> optin{0};
   gl_smem_optin(optin, kern, smem);
-  kern<<<grid, NT, smem, stream>>>(args);
+  if (!pdl) {
+    kern<<<grid, NT, smem, stream>>>(args);
+    return;
+  }
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(NT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, args);
 }
 
 #define GL_ENTRY3(R1, R2, R3, LANES, NT, INV)                                                 \

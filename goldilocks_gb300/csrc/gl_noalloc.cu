@@ -124,7 +124,7 @@ extern "C" int gl_ntt_noalloc(uint64_t *data, uint64_t len, int dir, void *strea
   a.tw_lo = tab + GL_NOALLOC_TLO;
   a.tw_hi = tab + GL_NOALLOC_THI;
   a.tw_unscale = inv ? gl_to_mont(len % GL_P) : 0;  // tw_lo carries 1/len
-  kc->launch(a, dim3((unsigned)gl_tiles(n2, kc)), stream);
+  kc->launch(a, dim3((unsigned)gl_tiles(n2, kc)), stream, false);
 
   gl_pass_args b{};  // row pass: scratch -> data at the transposed position
   b.in = p.scratch; b.out = data;
@@ -134,7 +134,7 @@ extern "C" int gl_ntt_noalloc(uint64_t *data, uint64_t len, int dir, void *strea
   b.in_limit = 0xffffffffu;
   b.tw_lane_div = 1;
   b.tw_m = b.tw_r2 = tab + GL_NOALLOC_T2;
-  kr->launch(b, dim3((unsigned)gl_tiles(n1, kr)), stream);
+  kr->launch(b, dim3((unsigned)gl_tiles(n1, kr)), stream, true);  // follows kc on the stream
 
   return gl_cuda_status(cudaGetLastError());
 }

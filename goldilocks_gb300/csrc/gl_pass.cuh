@@ -30,6 +30,23 @@ enum : uint32_t {
   GL_PF_CANON_IN = 1024u,      // inputs may be >= p: reduce them on load (first pass of a call)
 };
 
+// Programmatic dependent launch (griddepcontrol, sm_90 and later).  A pass
+// launched with programmatic stream serialization may start once every CTA
+// of the previous kernel in its stream has started; it waits in gl_pdl_wait
+// -- until that kernel has finished and its writes are visible -- before it
+// reads data or writes global memory.  Without that launch attribute both are
+// no-ops.
+__device__ __forceinline__ void gl_pdl_launch_dependents() {
+#if defined(__CUDA_ARCH__)
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+__device__ __forceinline__ void gl_pdl_wait() {
+#if defined(__CUDA_ARCH__)
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+
 struct gl_pass_args {
   const uint64_t *in;
   uint64_t *out;

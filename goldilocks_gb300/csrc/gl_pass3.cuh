@@ -68,6 +68,34 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
   constexpr int S1 = R2 * R3;
 
   const int64_t lane0 = bx * LANES;
+  gl_pdl_launch_dependents();
+
+  // Stage the round-2 twiddles and the pass-twiddle steps (read after the
+  // barrier that ends round 1).  They come from constant tables, so they are
+  // loaded before the wait below and their latency overlaps the previous
+  // pass's tail (under programmatic dependent launch) and this pass's loads.
+  constexpr int SL = L::NR == 3 ? R1 * R2 : R1;  // output stride of the last digit
+  const bool tw_steps = (a.flags & (GL_PF_PASS_TWIDDLE | GL_PF_TW_TABLE)) == GL_PF_PASS_TWIDDLE;
+  if constexpr (L::NR > 1) {
+    if constexpr (L::NT2 > 0) {
+      for (int i = threadIdx.x; i < L::NT2; i += NT) gl_sm_st(a, sm, L::T2 + i, L::WORDS, __ldg(a.tw_r2 + R1 * i));
+    }
+    if (tw_steps) {
+      for (int i = threadIdx.x; i < L::NSTEP; i += NT) {
+        const int c = i / L::SS, t = i % L::SS;
+        if (t >= L::RL) continue;
+        if (lane0 + c >= (int64_t)a.lanes) continue;  // lanes past the end read no table
+        const uint64_t col = (uint64_t)(lane0 + c) / a.tw_lane_div + a.tw_col0;
+        uint64_t v = gl_tw2m(a.tw_lo, a.tw_hi, col * (uint64_t)(SL * t));
+        if (a.tw_unscale) v = gl_mont_mul(v, a.tw_unscale);
+        gl_sm_st(a, sm, L::STEP + i, L::WORDS, v);
+      }
+    }
+  }
+  // Everything below reads data an earlier kernel of the stream may write,
+  // or writes global memory.
+  gl_pdl_wait();
+
   const bool ptr_table = (a.flags & GL_PF_PTR_TABLE) != 0;
   const uint64_t *in = ptr_table ? a.in_ptrs[by] + bz * a.in_bs2 : a.in + by * a.in_bs + bz * a.in_bs2;
   uint64_t *out = ptr_table ? a.out_ptrs[by] + bz * a.out_bs2 : a.out + by * a.out_bs + bz * a.out_bs2;
@@ -149,24 +177,6 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
     }
   }
   if constexpr (L::NR == 1) return;
-  // Stage the round-2 twiddles and the pass-twiddle steps (read after the
-  // barrier below).
-  constexpr int SL = L::NR == 3 ? R1 * R2 : R1;  // output stride of the last digit
-  const bool tw_steps = (a.flags & (GL_PF_PASS_TWIDDLE | GL_PF_TW_TABLE)) == GL_PF_PASS_TWIDDLE;
-  if constexpr (L::NT2 > 0) {
-    for (int i = threadIdx.x; i < L::NT2; i += NT) gl_sm_st(a, sm, L::T2 + i, L::WORDS, __ldg(a.tw_r2 + R1 * i));
-  }
-  if (tw_steps) {
-    for (int i = threadIdx.x; i < L::NSTEP; i += NT) {
-      const int c = i / L::SS, t = i % L::SS;
-      if (t >= L::RL) continue;
-      if (lane0 + c >= (int64_t)a.lanes) continue;  // lanes past the end read no table
-      const uint64_t col = (uint64_t)(lane0 + c) / a.tw_lane_div + a.tw_col0;
-      uint64_t v = gl_tw2m(a.tw_lo, a.tw_hi, col * (uint64_t)(SL * t));
-      if (a.tw_unscale) v = gl_mont_mul(v, a.tw_unscale);
-      gl_sm_st(a, sm, L::STEP + i, L::WORDS, v);
-    }
-  }
   __syncthreads();  // uniform: every thread of the CTA reaches it
 
   // ------------------------------------------------------------- round 2

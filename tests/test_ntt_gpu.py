@@ -53,7 +53,11 @@ def test_pinned_host_memory_in_place(gl, oracle, cuda, n, count):
     assert np.array_equal(h, x)
 
 
-@pytest.mark.parametrize("n,count", [(8, 1000), (64, 333), (1024, 37), (4096, 9), (1 << 14, 5)])
+# Whole-transform lengths 512-4096 run one transform per CTA while the wider
+# kernel would leave SMs without a CTA (fewer than 4 x 152 transforms of
+# 1024-4096 points, 8 x 152 of 512) and the wide kernel above that.
+@pytest.mark.parametrize("n,count", [(8, 1000), (64, 333), (1024, 37), (4096, 9), (1 << 14, 5),
+                                     (2048, 1), (512, 3), (4096, 700), (1024, 650), (512, 1300)])
 def test_batched_plan(gl, oracle, cuda, n, count):
     x = rand_field(n * count, seed=count)
     d = to_dev(cuda, x)
