@@ -2,7 +2,7 @@
 recmo/goldilocks' `goldilocks-ntt` crate behind a C ABI (include/goldilocks_gpu.h).
 """
 from .ntt import (MODULUS, GoldilocksError, Plan, bit_reverse, clear_cache, convolve, divisors, fill_uniform,
-                  host_pipeline, intt, is_divisor, next, ntt, split, strategy, transpose)
+                  host_pipeline, host_pipeline_submit, intt, is_divisor, next, ntt, split, strategy, transpose)
 
 __all__ = ["MODULUS", "GoldilocksError", "Plan", "bit_reverse", "clear_cache", "convolve", "divisors",
-           "fill_uniform", "host_pipeline", "intt", "is_divisor", "next", "ntt", "split", "strategy", "transpose"]
+           "fill_uniform", "host_pipeline", "host_pipeline_submit", "intt", "is_divisor", "next", "ntt", "split", "strategy", "transpose"]

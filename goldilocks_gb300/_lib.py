@@ -37,6 +37,8 @@ SIGNATURES = [
     ("gl_coset_lde", _int, [_vp, _vp, _u64, _u64, _u32, _u64, _int, _vp]),
     ("gl_convolve", _int, [_vp, _vp, _u64, _u64, _u64, _int, _int, _vp]),
     ("gl_host_pipeline", _int, [_vp, _u64, _u32]),
+    ("gl_host_pipeline_submit", _int, [_vp, _u64, _u32, _vp]),
+    ("gl_host_pipeline_wait", _int, [_vp]),
     ("gl_batch_wait_selftest", _int, [_u64, ctypes.POINTER(_u32)]),
     ("gl_debug_inject_alloc_failures", _int, [_int]),
     ("gl_debug_field_op", _int, [_int, _vp, _vp, _vp, _u64, _vp]),

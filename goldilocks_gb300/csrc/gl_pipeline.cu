@@ -75,8 +75,16 @@ struct events {
 
 }  // namespace
 
-extern "C" int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_t depth) {
-  GL_NVTX("gl_host_pipeline");
+// Queues every copy and pass of the jobs on the library's four streams and
+// records *fin on the copy-out stream once all of them are done.  Nothing
+// here waits for the device, so the work of a later call overlaps this one's:
+// its copy-ins follow this call's copy-ins and its passes this call's passes
+// (each call has its own device block, allocated on the copy-in stream and
+// freed on the copy-out stream).  On an error return the streams have been
+// drained and *fin is not set.
+static int pipeline_enqueue(const gl_host_job *jobs, uint64_t njobs, uint32_t depth,
+                            cudaEvent_t *fin) {
+  *fin = nullptr;
   if (njobs == 0) return GL_OK;
   if (!jobs) return GL_ERR_INVALID;
   if (depth == 0) depth = 3;
@@ -105,18 +113,18 @@ extern "C" int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_
   const int ncomp = njobs > 1 ? kComp : 1;
   const uint64_t words = depth * slot_words + ncomp * scratch_words;
   cudaStream_t comp0 = ps->comp[0];
-  cudaError_t e = gl_malloc_async((void **)&block, std::max<uint64_t>(words, 1) * 8, comp0);
+  cudaError_t e = gl_malloc_async((void **)&block, std::max<uint64_t>(words, 1) * 8, ps->in);
   if (e != cudaSuccess) return gl_cuda_status(e);
-  events ready, done, freed, alloc, col_done;
+  events ready, done, freed, alloc, col_done, last;
   if ((st = ready.make(njobs)) != GL_OK || (st = done.make(njobs)) != GL_OK ||
       (st = freed.make(njobs)) != GL_OK || (st = alloc.make(1)) != GL_OK ||
-      (st = col_done.make(njobs)) != GL_OK) {
-    cudaFreeAsync(block, comp0);
+      (st = col_done.make(njobs)) != GL_OK || (st = last.make(kComp + 1)) != GL_OK) {
+    cudaFreeAsync(block, ps->in);
     return st;
   }
-  cudaEventRecord(alloc.ev[0], comp0);  // the block exists for the other streams
-  cudaStreamWaitEvent(ps->in, alloc.ev[0], 0);
-  cudaStreamWaitEvent(ps->comp[1], alloc.ev[0], 0);
+  cudaEventRecord(alloc.ev[0], ps->in);  // the block exists for the other streams
+  for (int c = 0; c < kComp; c++) cudaStreamWaitEvent(ps->comp[c], alloc.ev[0], 0);
+  cudaStreamWaitEvent(ps->out, alloc.ev[0], 0);
   std::vector<cudaEvent_t> chunk_ev;  // per chunked job: kChunks copy-ins, then kChunks row passes
   for (uint64_t i = 0; i < njobs && st == GL_OK; i++) {
     const gl_host_job &j = jobs[i];
@@ -202,27 +210,66 @@ extern "C" int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_
     if (e != cudaSuccess) st = gl_cuda_status(e);
     cudaEventRecord(freed.ev[i], ps->out);
   }
-  // The block is freed on the first compute stream once every copy-out and
-  // the other compute stream are done.
-  cudaEvent_t last[kComp] = {nullptr, nullptr};
-  for (int c = 0; c < kComp; c++) {
-    if (cudaEventCreateWithFlags(&last[c], cudaEventDisableTiming) != cudaSuccess) { last[c] = nullptr; continue; }
-    cudaEventRecord(last[c], c == 0 ? ps->out : ps->comp[c]);
-    cudaStreamWaitEvent(comp0, last[c], 0);
+  // The block is freed on the copy-out stream once the other streams are
+  // done with it; *fin marks the end of the call's work on all four.
+  for (int c = 0; c <= kComp; c++) {
+    cudaEventRecord(last.ev[c], c < kComp ? ps->comp[c] : ps->in);
+    cudaStreamWaitEvent(ps->out, last.ev[c], 0);
   }
-  cudaFreeAsync(block, comp0);
-  cudaError_t e1 = cudaStreamSynchronize(ps->in);
-  cudaError_t e2 = cudaStreamSynchronize(ps->out);
-  cudaError_t e3 = cudaSuccess;
-  for (int c = 0; c < kComp; c++) {
-    const cudaError_t ec = cudaStreamSynchronize(ps->comp[c]);
-    if (e3 == cudaSuccess) e3 = ec;
+  cudaFreeAsync(block, ps->out);
+  cudaEvent_t f = nullptr;
+  if (st == GL_OK) {
+    if ((e = cudaEventCreateWithFlags(&f, cudaEventDisableTiming)) != cudaSuccess) st = gl_cuda_status(e);
+    else if ((e = cudaEventRecord(f, ps->out)) != cudaSuccess) st = gl_cuda_status(e);
   }
-  for (int c = 0; c < kComp; c++)
-    if (last[c]) cudaEventDestroy(last[c]);
+  // Events still pending are released by CUDA once they complete; the waits
+  // already queued on them stand.
   for (auto ev : chunk_ev) cudaEventDestroy(ev);
+  if (st != GL_OK) {
+    if (f) cudaEventDestroy(f);
+    cudaStreamSynchronize(ps->in);
+    for (int c = 0; c < kComp; c++) cudaStreamSynchronize(ps->comp[c]);
+    cudaStreamSynchronize(ps->out);
+    return st;
+  }
+  *fin = f;
+  return GL_OK;
+}
+
+extern "C" int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_t depth) {
+  GL_NVTX("gl_host_pipeline");
+  cudaEvent_t fin = nullptr;
+  int st = pipeline_enqueue(jobs, njobs, depth, &fin);
+  if (st != GL_OK || !fin) return st;
+  cudaError_t e = cudaEventSynchronize(fin);
+  cudaEventDestroy(fin);
+  return gl_cuda_status(e);
+}
+
+struct gl_pipe_ticket {
+  cudaEvent_t fin;
+};
+
+extern "C" int gl_host_pipeline_submit(const gl_host_job *jobs, uint64_t njobs, uint32_t depth,
+                                       gl_pipe_ticket **ticket) {
+  GL_NVTX("gl_host_pipeline_submit");
+  if (!ticket) return GL_ERR_INVALID;
+  *ticket = nullptr;
+  cudaEvent_t fin = nullptr;
+  int st = pipeline_enqueue(jobs, njobs, depth, &fin);
   if (st != GL_OK) return st;
-  if (e1 != cudaSuccess) return gl_cuda_status(e1);
-  if (e2 != cudaSuccess) return gl_cuda_status(e2);
-  return gl_cuda_status(e3);
+  *ticket = new gl_pipe_ticket{fin};
+  return GL_OK;
+}
+
+extern "C" int gl_host_pipeline_wait(gl_pipe_ticket *ticket) {
+  GL_NVTX("gl_host_pipeline_wait");
+  if (!ticket) return GL_ERR_INVALID;
+  cudaError_t e = cudaSuccess;
+  if (ticket->fin) {
+    e = cudaEventSynchronize(ticket->fin);
+    cudaEventDestroy(ticket->fin);
+  }
+  delete ticket;
+  return gl_cuda_status(e);
 }

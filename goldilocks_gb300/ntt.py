@@ -155,13 +155,9 @@ def convolve(a, b_hat, size=None, montgomery=True):
     return a
 
 
-def host_pipeline(jobs, depth=0):
-    """Transform host buffers with the copies overlapped: `jobs` is a list of
-    (numpy uint64 array, size, [directions...]) -- each array holds
-    len/size transforms and gets the listed transforms (ntt/intt by
-    "fwd"/"inv") in order, in place, with one copy in and one copy out."""
+def _host_jobs(jobs):
+    """ctypes gl_host_job array for host_pipeline / host_pipeline_submit."""
     arr = (L.HostJob * max(len(jobs), 1))()
-    keep = []
     for i, (a, size, dirs) in enumerate(jobs):
         if not isinstance(a, np.ndarray) or a.dtype != np.uint64 or not a.flags.c_contiguous:
             raise TypeError("jobs need C-contiguous numpy uint64 arrays")
@@ -169,15 +165,60 @@ def host_pipeline(jobs, depth=0):
             raise ValueError("array length is not a multiple of the transform size")
         if len(dirs) > L.GL_HOST_JOB_MAX_OPS:
             raise ValueError("at most %d transforms per job" % L.GL_HOST_JOB_MAX_OPS)
-        keep.append(a)
         arr[i].data = a.ctypes.data if a.size else None
         arr[i].len, arr[i].count, arr[i].nops = size, a.size // size, len(dirs)
         for k, d in enumerate(dirs):
             arr[i].dirs[k] = L.GL_INVERSE if d in ("inv", L.GL_INVERSE) else L.GL_FORWARD
-    st = L.load().gl_host_pipeline(ctypes.addressof(arr), len(jobs), depth)
+    return arr
+
+
+def _host_jobs_check(st, jobs, what):
     bad = [s for _, s, _ in jobs if not is_divisor(s)]
-    _check(st, "host_pipeline", size=bad[0] if bad else None)
+    _check(st, what, size=bad[0] if bad else None)
+
+
+def host_pipeline(jobs, depth=0):
+    """Transform host buffers with the copies overlapped: `jobs` is a list of
+    (numpy uint64 array, size, [directions...]) -- each array holds
+    len/size transforms and gets the listed transforms (ntt/intt by
+    "fwd"/"inv") in order, in place, with one copy in and one copy out."""
+    arr = _host_jobs(jobs)
+    st = L.load().gl_host_pipeline(ctypes.addressof(arr), len(jobs), depth)
+    _host_jobs_check(st, jobs, "host_pipeline")
     return [a for a, _, _ in jobs]
+
+
+class PipelineTicket:
+    """A host_pipeline call in flight (host_pipeline_submit).  wait() returns
+    the arrays once they hold their results; until then they must not be
+    read, written or freed (the ticket keeps them alive)."""
+
+    def __init__(self, handle, arrays):
+        self._h = handle
+        self._arrays = arrays
+
+    def wait(self):
+        if self._h is None:
+            raise RuntimeError("host pipeline ticket already waited on")
+        h, self._h = self._h, None
+        _check(L.load().gl_host_pipeline_wait(h), "host_pipeline_wait")
+        return self._arrays
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None:
+            L.load().gl_host_pipeline_wait(self._h)  # never leave copies into freed arrays
+
+
+def host_pipeline_submit(jobs, depth=0):
+    """host_pipeline without the wait: queues the jobs and returns a
+    PipelineTicket.  Calls submitted back to back overlap (the next call's
+    copy-ins run while this one computes and copies out); calls in flight
+    must not share an array."""
+    arr = _host_jobs(jobs)
+    h = ctypes.c_void_p()
+    st = L.load().gl_host_pipeline_submit(ctypes.addressof(arr), len(jobs), depth, ctypes.byref(h))
+    _host_jobs_check(st, jobs, "host_pipeline_submit")
+    return PipelineTicket(h.value, [a for a, _, _ in jobs])
 
 
 def transpose(values, shape):

@@ -166,6 +166,19 @@ typedef struct {
  * gl_plan_execute per transform. */
 int gl_host_pipeline(const gl_host_job *jobs, uint64_t njobs, uint32_t depth);
 
+/* gl_host_pipeline without the wait: queues the jobs and returns at once with
+ * a ticket; gl_host_pipeline_wait(ticket) returns when every buffer of that
+ * call holds its result, and frees the ticket (wait on each ticket exactly
+ * once).  Calls submitted back to back overlap: the next call's copy-ins run
+ * while this call computes and copies out, so a stream of batches keeps both
+ * link directions and the SMs busy.  The buffers of a call must stay valid
+ * and untouched until its wait returns; two calls in flight must not share a
+ * buffer.  Invalid jobs are refused before anything is queued (no ticket). */
+typedef struct gl_pipe_ticket gl_pipe_ticket;
+int gl_host_pipeline_submit(const gl_host_job *jobs, uint64_t njobs, uint32_t depth,
+                            gl_pipe_ticket **ticket);
+int gl_host_pipeline_wait(gl_pipe_ticket *ticket);
+
 /* ---- K12 Merkle layers and proof of work (pcs/src/k12, pcs/src/pow.rs) ----
  *
  * Byte-oriented; `mem` applies to every data buffer of a call (the 32-byte

@@ -58,3 +58,30 @@ def test_pipeline_errors(gl, cuda):
     with pytest.raises(ValueError, match="at most"):
         gl.host_pipeline([(x, 16, ("fwd",) * 5)])
     gl.host_pipeline([])
+
+
+def test_submitted_calls_overlap_and_match_oracle(gl, oracle, cuda):
+    """Three host_pipeline_submit calls in flight at once (the later ones'
+    copy-ins run beside the earlier ones' passes and copy-outs), each on its
+    own buffers, waited on out of order."""
+    calls = [[(1 << 22, ("fwd", "inv")), (1 << 16, ("fwd",))],
+             [(16711680, ("fwd",)), (4096 * 3, ("inv",))],
+             [(1 << 20, ("inv", "fwd")), (1 << 22, ("fwd",))]]
+    xs, tickets, jobs_of = [], [], []
+    for c, specs in enumerate(calls):
+        jobs = []
+        for i, (n, dirs) in enumerate(specs):
+            x = gl.fill_uniform(n, seed=0x5B + 10 * c + i)
+            xs.append((x, n, dirs))
+            jobs.append((pinned(cuda, x), n, dirs))
+        jobs_of.append(jobs)
+        tickets.append(gl.host_pipeline_submit(jobs))
+    outs = [None] * len(tickets)
+    for c in (1, 0, 2):
+        outs[c] = tickets[c].wait()
+    got = [h for o in outs for h in o]
+    for h, (x, n, dirs) in zip(got, xs):
+        want = x
+        for d in dirs:
+            want = (oracle.ntt if d == "fwd" else oracle.intt)(want)
+        assert np.array_equal(h, want), (n, dirs)

@@ -40,3 +40,27 @@ def test_c_abi_rejects_bad_jobs(gl):
     assert lib.gl_host_pipeline(ctypes.addressof(job), 1, 0) == L.GL_ERR_INVALID
     assert lib.gl_host_pipeline(None, 1, 0) == L.GL_ERR_INVALID
     assert lib.gl_host_pipeline(None, 0, 0) == L.GL_OK  # nothing to do
+
+
+def test_submit_rejects_bad_jobs_without_a_ticket(gl):
+    L = gl._lib
+    lib = L.load()
+    x = np.zeros(16, dtype=np.uint64)
+    job = L.HostJob()
+    job.data, job.len, job.count, job.nops = x.ctypes.data, 16, 1, 1
+    job.dirs[0] = 5
+    t = ctypes.c_void_p(1234)
+    assert lib.gl_host_pipeline_submit(ctypes.addressof(job), 1, 0, ctypes.byref(t)) == L.GL_ERR_INVALID
+    assert t.value is None                               # no ticket for a refused call
+    job.dirs[0] = L.GL_FORWARD
+    assert lib.gl_host_pipeline_submit(ctypes.addressof(job), 1, 0, None) == L.GL_ERR_INVALID
+    assert lib.gl_host_pipeline_wait(None) == L.GL_ERR_INVALID
+    # nothing to do: a ticket that is already complete
+    assert lib.gl_host_pipeline_submit(None, 0, 0, ctypes.byref(t)) == L.GL_OK and t.value
+    assert lib.gl_host_pipeline_wait(t) == L.GL_OK
+    with pytest.raises(ValueError, match="not a supported NTT size"):
+        gl.host_pipeline_submit([(np.arange(14, dtype=np.uint64), 7, ("fwd",))])
+    tk = gl.host_pipeline_submit([])
+    assert tk.wait() == []
+    with pytest.raises(RuntimeError, match="already waited"):
+        tk.wait()
