@@ -499,7 +499,6 @@ def run_ours(args):
 
     clocks = ClockSampler(local)
     clocks.start()
-    lib.gl_profile_enable(1)
     evs = []
     torch.cuda.synchronize()
     if dist:
@@ -519,6 +518,17 @@ def run_ours(args):
         dist.barrier()
     clk = clocks.stop()
     total_ms = sum(a.elapsed_time(b) for a, b in evs)
+    # Per-kernel launch times: the same steps again, every launch bracketed by
+    # CUDA events on its stream (the library's profile).  Kept out of the steps
+    # timed above: an event between two passes stops the second from starting
+    # early (programmatic dependent launch), so bracketed steps run slower.
+    lib.gl_profile_enable(1)
+    gc.disable()
+    for _ in range(args.steps):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    gc.enable()
     n_ent = lib.gl_profile_read(None, 0)
     ents = (L.ProfileEntry * max(n_ent, 1))()
     lib.gl_profile_read(ents, n_ent)
@@ -604,7 +614,7 @@ def run_ours(args):
             pend.wait()
             if marks is not None:
                 marks.append(time.perf_counter())
-        run(4)
+        run(8)
         if dist:
             dist.barrier()
         gc.collect()
@@ -618,9 +628,13 @@ def run_ours(args):
             gc.enable()
         step_ms[name] = [round((b - a) * 1e3, 3) for a, b in zip([t0] + marks[:-1], marks)]
         return max_over_ranks(dist, total, "cuda")
-    e2e_s = timed_stream("stream")
-    sync_s = timed(host_step, "pipeline")
+    # The per-call and one-step-at-a-time forms run first: on a fresh box the
+    # first tens of milliseconds of copies from newly pinned host memory ran
+    # slower (stream steps of 2.5 ms instead of 1.9 ms right after the device
+    # steps above, 1.9 ms once warm), and they warm that up for the stream.
     per_call_s = timed(host_step_per_call, "per_call")
+    sync_s = timed(host_step, "pipeline")
+    e2e_s = timed_stream("stream")
     # Every step was a forward and an inverse transform: the buffers must hold
     # their inputs again.
     checked = all(np.array_equal(h, gl.fill_uniform(n, seed=seed + i))
@@ -661,6 +675,9 @@ def run_ours(args):
                                               "these sources, profiles/ncu_pass_kernels.json) x elements per launch",
                     "algorithmic_bytes_per_launch": 16.0 * per_launch_el,
                     "mean_launch_ms": mean_ms,
+                    "launch_times": "CUDA events around every launch, on its stream, over a second run of "
+                                    "the same %d steps (launches bracketed, so without programmatic "
+                                    "dependent launch)" % args.steps,
                     "share": dom["total_ms"] / max(sum(p["total_ms"] for p in prof), 1e-12)}
     # The bound the passes actually meet: instruction issue (4 warp
     # instructions per SM per clock), from the ncu instruction count per
