@@ -723,9 +723,12 @@ extern "C" void gl_plan_release(gl_plan *) {}
 static std::vector<gl_plan *> g_retired;  // guarded by g_cache_mu
 
 extern "C" void gl_clear_cache(void) {
-  std::lock_guard<std::mutex> lk(g_cache_mu);
-  for (auto &kv : g_cache) g_retired.push_back(kv.second);
-  g_cache.clear();
+  {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    for (auto &kv : g_cache) g_retired.push_back(kv.second);
+    g_cache.clear();
+  }
+  gl_pipeline_release_blocks();
 }
 
 gl_plan *gl_plan_from_choice(uint64_t size, const gl_choice &c) {

@@ -172,6 +172,7 @@ void gl_launch(const gl_kernel_entry *k, int role, const gl_pass_args &a, dim3 g
 int gl_cuda_status(cudaError_t e);
 void gl_init_mempool_once();
 int gl_sm_count();  // multiprocessors of the current device
+void gl_pipeline_release_blocks();  // idle device blocks cached by gl_host_pipeline (gl_pipeline.cu)
 
 // Optional load-side transformation (the LDE's zero padding and coset shift).
 struct gl_load_opts {

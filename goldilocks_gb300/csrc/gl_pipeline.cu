@@ -27,12 +27,68 @@ namespace {
 // idle.  Jobs alternate between two scratch buffers.
 constexpr int kComp = 2;
 
+// A device block (slots and scratch) of a call, kept for later calls: reused
+// once the event recorded after its last use has completed.  The library
+// pool does not hand a block freed on the copy-out stream to an allocation on
+// the copy-in stream until long after the free has completed: a stream of
+// calls grew it by one block per call (13 GB over 20 calls of the bench's
+// four buffers) and each call spent about 1.5 ms of host time mapping the new
+// memory, which starved the device.
+struct pipe_block {
+  uint64_t *p = nullptr;
+  uint64_t words = 0;
+  cudaEvent_t idle = nullptr;
+};
+constexpr size_t kKeepBlocks = 3;  // two calls in flight and one being queued
+
 struct pipe_streams {
   cudaStream_t in = nullptr, out = nullptr;
   cudaStream_t comp[kComp] = {nullptr, nullptr};
   std::mutex mu;  // one pipeline per device at a time
   cudaEvent_t tail = nullptr;  // recorded at the end of every call's work (under mu)
+  std::vector<pipe_block> blocks;  // under mu
 };
+
+bool block_idle(const pipe_block &b) { return cudaEventQuery(b.idle) == cudaSuccess; }
+
+// Index of an idle cached block of at least `words`, else of a new block
+// allocated on the copy-in stream (idle blocks too small for it are freed);
+// -1 with *err set when the allocation fails.
+long take_block(pipe_streams *ps, uint64_t words, cudaError_t *err) {
+  for (size_t b = 0; b < ps->blocks.size(); b++)
+    if (ps->blocks[b].words >= words && block_idle(ps->blocks[b])) return (long)b;
+  for (size_t b = 0; b < ps->blocks.size();) {
+    if (ps->blocks[b].words < words && block_idle(ps->blocks[b])) {
+      cudaFreeAsync(ps->blocks[b].p, ps->in);
+      cudaEventDestroy(ps->blocks[b].idle);
+      ps->blocks.erase(ps->blocks.begin() + b);
+    } else {
+      b++;
+    }
+  }
+  pipe_block nb;
+  nb.words = words;
+  if ((*err = gl_malloc_async((void **)&nb.p, words * 8, ps->in)) != cudaSuccess) return -1;
+  if ((*err = cudaEventCreateWithFlags(&nb.idle, cudaEventDisableTiming)) != cudaSuccess) {
+    cudaFreeAsync(nb.p, ps->in);
+    return -1;
+  }
+  ps->blocks.push_back(nb);
+  return (long)ps->blocks.size() - 1;
+}
+
+// After a call's work is queued: the block becomes idle when `s` reaches this
+// point; beyond kKeepBlocks cached blocks, the block is freed instead.
+void put_block(pipe_streams *ps, long bi, cudaStream_t s) {
+  pipe_block &b = ps->blocks[(size_t)bi];
+  if (ps->blocks.size() > kKeepBlocks) {
+    cudaFreeAsync(b.p, s);
+    cudaEventDestroy(b.idle);
+    ps->blocks.erase(ps->blocks.begin() + bi);
+    return;
+  }
+  cudaEventRecord(b.idle, s);
+}
 
 std::mutex g_pipe_mu;
 std::map<int, pipe_streams *> g_pipes;
@@ -116,13 +172,15 @@ static int pipeline_enqueue(const gl_host_job *jobs, uint64_t njobs, uint32_t de
   const int ncomp = njobs > 1 ? kComp : 1;
   const uint64_t words = depth * slot_words + ncomp * scratch_words;
   cudaStream_t comp0 = ps->comp[0];
-  cudaError_t e = gl_malloc_async((void **)&block, std::max<uint64_t>(words, 1) * 8, ps->in);
-  if (e != cudaSuccess) return gl_cuda_status(e);
+  cudaError_t e = cudaSuccess;
+  const long bi = take_block(ps, std::max<uint64_t>(words, 1), &e);
+  if (bi < 0) return gl_cuda_status(e);
+  block = ps->blocks[(size_t)bi].p;
   events ready, done, freed, alloc, col_done, last;
   if ((st = ready.make(njobs)) != GL_OK || (st = done.make(njobs)) != GL_OK ||
       (st = freed.make(njobs)) != GL_OK || (st = alloc.make(1)) != GL_OK ||
       (st = col_done.make(njobs)) != GL_OK || (st = last.make(kComp + 1)) != GL_OK) {
-    cudaFreeAsync(block, ps->in);
+    put_block(ps, bi, ps->in);
     return st;
   }
   cudaEventRecord(alloc.ev[0], ps->in);  // the block exists for the other streams
@@ -229,13 +287,14 @@ static int pipeline_enqueue(const gl_host_job *jobs, uint64_t njobs, uint32_t de
     if (e != cudaSuccess) st = gl_cuda_status(e);
     cudaEventRecord(freed.ev[i], ps->out);
   }
-  // The block is freed on the copy-out stream once the other streams are
-  // done with it; *fin marks the end of the call's work on all four.
+  // The block is idle once the copy-out stream, which waits for the other
+  // three, reaches this point; *fin marks the end of the call's work on all
+  // four.
   for (int c = 0; c <= kComp; c++) {
     cudaEventRecord(last.ev[c], c < kComp ? ps->comp[c] : ps->in);
     cudaStreamWaitEvent(ps->out, last.ev[c], 0);
   }
-  cudaFreeAsync(block, ps->out);
+  put_block(ps, bi, ps->out);
   if (!ps->tail && cudaEventCreateWithFlags(&ps->tail, cudaEventDisableTiming) != cudaSuccess)
     ps->tail = nullptr;
   if (ps->tail) cudaEventRecord(ps->tail, ps->out);
@@ -294,4 +353,22 @@ extern "C" int gl_host_pipeline_wait(gl_pipe_ticket *ticket) {
   }
   delete ticket;
   return gl_cuda_status(e);
+}
+
+// Frees the cached pipeline blocks that are idle (gl_clear_cache).
+void gl_pipeline_release_blocks() {
+  std::lock_guard<std::mutex> lk(g_pipe_mu);
+  for (auto &kv : g_pipes) {
+    pipe_streams *ps = kv.second;
+    std::lock_guard<std::mutex> pk(ps->mu);
+    for (size_t b = 0; b < ps->blocks.size();) {
+      if (block_idle(ps->blocks[b])) {
+        cudaFreeAsync(ps->blocks[b].p, ps->out);
+        cudaEventDestroy(ps->blocks[b].idle);
+        ps->blocks.erase(ps->blocks.begin() + b);
+      } else {
+        b++;
+      }
+    }
+  }
 }

@@ -103,7 +103,8 @@ int gl_plan_execute_ws(const gl_plan *plan, uint64_t *data, uint64_t len, int di
 int gl_ntt(uint64_t *values, uint64_t len, int mem, void *stream);
 /* ntt::intt: inverse transform in place (lengths 0 and 1 are no-ops). */
 int gl_intt(uint64_t *values, uint64_t len, int mem, void *stream);
-/* ntt::clear_cache: forget cached plans (handles already returned stay valid). */
+/* ntt::clear_cache: forget cached plans (handles already returned stay valid);
+ * also frees the idle device blocks gl_host_pipeline keeps for later calls. */
 void gl_clear_cache(void);
 
 /* ---- column batches and the coset LDE (no counterpart in the reference) ---- */
