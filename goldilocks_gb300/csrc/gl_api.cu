@@ -194,6 +194,12 @@ const gl_kernel_entry *gl_find_kernel_cols(uint64_t m, bool inv) {
   return gl_find_kernel4(m, inv);
 }
 
+const gl_kernel_entry *gl_find_kernel_gt(uint64_t m, bool inv) {
+  size_t cnt = 0;
+  const gl_kernel_entry *e = inv ? gl_kernels_gt17_inv(&cnt) : gl_kernels_gt17_fwd(&cnt);
+  return find_in(e, cnt, m);
+}
+
 const gl_kernel_entry *gl_find_kernel4(uint64_t m, bool inv) {
   size_t cnt = 0;
   const gl_kernel_entry *e = inv ? gl_kernels_pass_inv(&cnt) : gl_kernels_pass_fwd(&cnt);
@@ -220,6 +226,7 @@ extern "C" int gl_preload_kernels(void) {
   std::vector<const void *> funcs;
   using table_fn = const gl_kernel_entry *(*)(size_t *);
   for (table_fn f : {gl_kernels_full_fwd, gl_kernels_full_inv, gl_kernels_full1_fwd, gl_kernels_full1_inv,
+                     gl_kernels_gt17_fwd, gl_kernels_gt17_inv,
                      gl_kernels_pass_fwd, gl_kernels_pass_inv,
                      gl_kernels_mixed35_fwd, gl_kernels_mixed35_inv, gl_kernels_mixed17_fwd,
                      gl_kernels_mixed17_inv, gl_kernels_pass2_fwd, gl_kernels_pass2_inv, gl_kernels_cols_fwd,
@@ -462,6 +469,14 @@ bool gl_choice_apply(gl_plan *pl, const gl_choice &c) {
     for (int s = 0; c.kind >= 2 && s < c.kind; s++) {
       pl->k[s][d] = c.lanes4 ? gl_find_kernel4(f[s], d == 1) : gl_find_kernel(f[s], false, d == 1);
       pl->k4[s][d] = gl_find_kernel_cols(f[s], d == 1);
+    }
+    // The last pass (rows: no pass twiddle) in the Good-Thomas form where one
+    // is compiled for its size.
+    if (c.kind >= 2) {
+      if (const gl_kernel_entry *g = gl_find_kernel_gt(f[c.kind - 1], d == 1)) {
+        pl->k[c.kind - 1][d] = g;
+        pl->k4[c.kind - 1][d] = g;
+      }
     }
   }
   return true;
@@ -779,7 +794,8 @@ extern "C" int gl_plan_describe(const gl_plan *plan, char *buf, size_t cap) {
   std::string s = plan->tree + " | gpu: ";
   auto kname = [](const gl_kernel_entry *k) {
     std::string t = kernel_shape(k);
-    t.insert(t.size() - 1, ", " + std::to_string(k->lanes) + " lanes" + (k->generic ? ", run-time radices" : ""));
+    t.insert(t.size() - 1, ", " + std::to_string(k->lanes) + " lanes" + (k->generic ? ", run-time radices" : "") +
+                               (k->gt ? ", Good-Thomas" : ""));
     return t;
   };
   if (plan->kind == 0) s += "no-op";

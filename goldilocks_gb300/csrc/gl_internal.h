@@ -47,6 +47,7 @@ struct gl_kernel_entry {
   gl_launch_fn launch;
   bool generic = false;  // gl_generic_kernel: radices passed at run time
   const void *func = nullptr;  // the __global__ function (gl_preload_kernels)
+  bool gt = false;             // Good-Thomas inner transform: no pass twiddle allowed
 };
 
 // Kernel sets compiled in separate translation units (parallel build).
@@ -59,6 +60,12 @@ const gl_kernel_entry *gl_kernels_full1_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_full1_inv(size_t *count);
 const gl_kernel_entry *gl_kernels_pass_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_pass_inv(size_t *count);
+// Passes with a Good-Thomas inner R2 x R3 transform (coprime R2, R3), for
+// the last pass of a plan (rows: no pass twiddle); only the shapes measured
+// faster than their Cooley-Tukey form are compiled.
+const gl_kernel_entry *gl_kernels_gt17_fwd(size_t *count);
+const gl_kernel_entry *gl_kernels_gt17_inv(size_t *count);
+const gl_kernel_entry *gl_find_kernel_gt(uint64_t m, bool inv);  // nullptr if none
 // Four-lane passes of mixed-radix sizes (factors 3 or 5; factor 17).
 const gl_kernel_entry *gl_kernels_mixed35_fwd(size_t *count);
 const gl_kernel_entry *gl_kernels_mixed35_inv(size_t *count);

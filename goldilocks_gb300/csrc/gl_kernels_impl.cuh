@@ -3,10 +3,10 @@
 #pragma once
 #include "gl_internal.h"
 
-template <int R1, int R2, int R3, int LANES, int NT, bool INV, int MINB = 1>
+template <int R1, int R2, int R3, int LANES, int NT, bool INV, int MINB = 1, bool GT = false>
 static void gl_launch_pass3(const gl_pass_args &args, dim3 grid, cudaStream_t stream, bool pdl) {
   constexpr size_t smem = gl_p3_smem_bytes<R1, R2, R3, LANES>();
-  auto kern = gl_pass3_kernel<R1, R2, R3, LANES, NT, INV, MINB>;
+  auto kern = gl_pass3_kernel<R1, R2, R3, LANES, NT, INV, MINB, GT>;
   static std::atomic<uint64_t> optin{0};
   gl_smem_optin(optin, kern, smem);
   if (!pdl) {
@@ -37,3 +37,10 @@ static void gl_launch_pass3(const gl_pass_args &args, dim3 grid, cudaStream_t st
   {R1 * R2 * R3, R1, R2, R3, LANES, INV, gl_p3_smem_bytes<R1, R2, R3, LANES>(), NT,          \
    gl_launch_pass3<R1, R2, R3, LANES, NT, INV, MINB>, false,                                  \
    (const void *)gl_pass3_kernel<R1, R2, R3, LANES, NT, INV, MINB>}
+
+// Good-Thomas inner transform (gcd(R2, R3) = 1): for passes without a pass
+// twiddle (rows, column batches); MINB as above.
+#define GL_ENTRY3G(R1, R2, R3, LANES, NT, MINB, INV)                                          \
+  {R1 * R2 * R3, R1, R2, R3, LANES, INV, gl_p3_smem_bytes<R1, R2, R3, LANES>(), NT,          \
+   gl_launch_pass3<R1, R2, R3, LANES, NT, INV, MINB, true>, false,                            \
+   (const void *)gl_pass3_kernel<R1, R2, R3, LANES, NT, INV, MINB, true>, true}

@@ -9,6 +9,15 @@
 //   round 3: DFT_R3 over d3 for each (k1, k2)
 //   output frequency k = k1 + R1*k2 + R1*R2*k3.
 //
+// GT variant (gcd(R2, R3) = 1; passes without a pass twiddle): the inner
+// R2*R3-point transform of rounds 2 and 3 is Good-Thomas instead of
+// Cooley-Tukey, so it needs no twiddles.  Round 2 gathers its inputs at
+// d' = (R3*a + R2*b) mod R2*R3 over a (b fixed) and writes its outputs k2
+// back to the same positions; round 3 gathers d' = (R3*k2 + R2*b) mod R2*R3
+// over b; the output frequency is k = k1 + R1*k', k' = CRT(k2 mod R2,
+// k3 mod R3).  (Adjacent threads take adjacent b in round 2 and adjacent k2
+// in round 3, so the gathers stay on distinct banks.)
+//
 // Each thread holds one radix-R group in registers (R <= 17), so the code per
 // round is one straight-line codelet and the kernel runs 1024 threads per
 // CTA.  Round 1 reads global memory directly and the last round writes it;
@@ -57,15 +66,33 @@ constexpr size_t gl_p3_smem_bytes() {
   return (size_t)gl_p3_layout<R1, R2, R3, LANES>::WORDS * 8;
 }
 
+// Good-Thomas constants of the inner R2 x R3 transform.
+constexpr int gl_gcd(int a, int b) { return b == 0 ? a : gl_gcd(b, a % b); }
+constexpr int gl_modinv(int a, int m) {  // a^-1 mod m, 0 when there is none
+  for (int r = 1; r < m; r++)
+    if ((a * r) % m == 1) return r;
+  return 0;
+}
+template <int R2, int R3>
+struct gl_gt_consts {
+  static constexpr int S = R2 * R3;
+  static constexpr int AINV = gl_modinv(R3 % R2, R2);  // a = d' * AINV mod R2
+  static constexpr int BINV = gl_modinv(R2 % R3, R3);  // b = d' * BINV mod R3
+  static constexpr int E2 = R3 * AINV;                 // 1 mod R2, 0 mod R3
+  static constexpr int E3 = R2 * BINV;                 // 0 mod R2, 1 mod R3
+};
+
 // One CTA's work: tile (bx, by, bz) of the pass described by `a`, with NT
 // threads and the dynamic shared memory `sm`.  Called by gl_pass3_kernel
 // (tile = blockIdx) and by the persistent batch kernel (tile from its queue).
-template <int R1, int R2, int R3, int LANES, int NT, bool INV>
+template <int R1, int R2, int R3, int LANES, int NT, bool INV, bool GT = false>
 __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int64_t by,
                                           int64_t bz, uint64_t *sm) {
   using L = gl_p3_layout<R1, R2, R3, LANES>;
+  using GTC = gl_gt_consts<R2, R3>;
   constexpr int M = L::M;
   constexpr int S1 = R2 * R3;
+  static_assert(!GT || (L::NR == 3 && gl_gcd(R2, R3) == 1), "Good-Thomas inner transform needs coprime R2, R3");
 
   const int64_t lane0 = bx * LANES;
   gl_pdl_launch_dependents();
@@ -77,7 +104,7 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
   constexpr int SL = L::NR == 3 ? R1 * R2 : R1;  // output stride of the last digit
   const bool tw_steps = (a.flags & (GL_PF_PASS_TWIDDLE | GL_PF_TW_TABLE)) == GL_PF_PASS_TWIDDLE;
   if constexpr (L::NR > 1) {
-    if constexpr (L::NT2 > 0) {
+    if constexpr (L::NT2 > 0 && !GT) {
       for (int i = threadIdx.x; i < L::NT2; i += NT) gl_sm_st(a, sm, L::T2 + i, L::WORDS, __ldg(a.tw_r2 + R1 * i));
     }
     if (tw_steps) {
@@ -187,6 +214,22 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
       const int k1 = g / R3, d3 = g % R3;
       const int base = k1 * S1 + d3;
       uint64_t x[R2];
+      if constexpr (GT) {
+        // inputs a at (R3*a + R2*b) mod S1, b = d3; outputs k2 = t in their place
+        int pos[R2];
+#pragma unroll
+        for (int t = 0; t < R2; t++) {
+          int v = R2 * d3 + R3 * t;
+          if (v >= S1) v -= S1;
+          pos[t] = k1 * S1 + v;
+        }
+#pragma unroll
+        for (int t = 0; t < R2; t++) x[t] = gl_sm_ld(a, sm, L::word(c, pos[t]), LANES * L::LS);
+        gl_dft<R2, INV>(x);
+#pragma unroll
+        for (int t = 0; t < R2; t++) gl_sm_st(a, sm, L::word(c, pos[t]), LANES * L::LS, x[t]);
+        continue;
+      }
 #pragma unroll
       for (int t = 0; t < R2; t++) x[t] = gl_sm_ld(a, sm, L::word(c, base + R3 * t), LANES * L::LS);
       gl_dft<R2, INV>(x);
@@ -214,16 +257,46 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
       if constexpr (L::NR == 3) {
         const int k1 = g / R2, k2 = g % R2;
         base = k1 * S1 + k2 * R3;
-        kbase = k1 + R1 * k2;
+        // GT: k = k1 + R1 * ((k2 * E2 + t * E3) mod S1); kbase holds k2 * E2 mod S1
+        kbase = GT ? (k2 * GTC::E2) % S1 : k1 + R1 * k2;
       } else {
         base = g * R2;
         kbase = g;
       }
       uint64_t x[RL];
+      if constexpr (GT) {
+        // inputs b at (R3*k2 + R2*b) mod S1 of block k1
+        const int k1 = g / R2, k2 = g % R2;
 #pragma unroll
-      for (int t = 0; t < RL; t++) x[t] = gl_sm_ld(a, sm, L::word(c, base + t), LANES * L::LS);
+        for (int t = 0; t < RL; t++) {
+          int v = R3 * k2 + R2 * t;
+          if (v >= S1) v -= S1;
+          x[t] = gl_sm_ld(a, sm, L::word(c, k1 * S1 + v), LANES * L::LS);
+        }
+      } else {
+#pragma unroll
+        for (int t = 0; t < RL; t++) x[t] = gl_sm_ld(a, sm, L::word(c, base + t), LANES * L::LS);
+      }
       gl_dft<RL, INV>(x);
       const int64_t lane = lane0 + c;
+      if constexpr (GT) {
+        // Rows and column batches only: no pass twiddle in this form.
+        if (lane < (int64_t)a.lanes) {
+          const int k1 = g / R2;
+          uint64_t *dst = out + lane * a.out_ls + (int64_t)k1 * a.out_is;
+          const int64_t kstride = (int64_t)R1 * a.out_is;
+          const bool mul = (a.flags & GL_PF_OUT_MUL) != 0;
+          const uint64_t *mb = mul ? a.mul + by * a.mul_bs + bz * a.mul_bs2 : nullptr;
+#pragma unroll
+          for (int t = 0; t < RL; t++) {
+            int kk = kbase + (t * GTC::E3) % S1;
+            if (kk >= S1) kk -= S1;
+            const uint64_t v = mul ? gl_out_mul(a, mb, lane, k1 + R1 * kk, x[t]) : x[t];
+            gl_st_out(a, dst + (int64_t)kk * kstride, v);
+          }
+        }
+        continue;
+      }
       if (lane < (int64_t)a.lanes) {
         uint64_t *dst = out + lane * a.out_ls;
         if (tw_steps) {
@@ -256,8 +329,8 @@ __device__ __forceinline__ void gl_block3(const gl_pass_args &a, int64_t bx, int
   }
 }
 
-template <int R1, int R2, int R3, int LANES, int NT, bool INV, int MINB = 1>
+template <int R1, int R2, int R3, int LANES, int NT, bool INV, int MINB = 1, bool GT = false>
 __global__ void __launch_bounds__(NT, MINB) gl_pass3_kernel(const gl_pass_args a) {
   extern __shared__ uint64_t sm[];
-  gl_block3<R1, R2, R3, LANES, NT, INV>(a, blockIdx.x, blockIdx.y, blockIdx.z, sm);
+  gl_block3<R1, R2, R3, LANES, NT, INV, GT>(a, blockIdx.x, blockIdx.y, blockIdx.z, sm);
 }

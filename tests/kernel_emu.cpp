@@ -38,7 +38,7 @@ static uint64_t g_tw_unscale = 0;  // gl_pass_args::tw_unscale of the next launc
 #include "gl_pass3.cuh"
 #include "gl_generic.cuh"
 
-template <int R1, int R2, int R3, int LANES, int NT, bool INV>
+template <int R1, int R2, int R3, int LANES, int NT, bool INV, bool GT = false>
 static void run_grid(const gl_pass_args &a, unsigned gx, unsigned gy, unsigned gz) {
   for (unsigned z = 0; z < gz; z++)
     for (unsigned y = 0; y < gy; y++)
@@ -51,7 +51,7 @@ static void run_grid(const gl_pass_args &a, unsigned gx, unsigned gy, unsigned g
         for (int t = 0; t < NT; t++)
           th.emplace_back([&a, t] {
             threadIdx.x = t;
-            gl_pass3_kernel<R1, R2, R3, LANES, NT, INV>(a);
+            gl_pass3_kernel<R1, R2, R3, LANES, NT, INV, 1, GT>(a);
           });
         for (auto &t : th) t.join();
       }
@@ -124,6 +124,33 @@ int emu_pass3(EMU_ARGS) {
   SHAPE(16, 17, 1, 64)
   SHAPE(8, 5, 17, 256)
   SHAPE(16, 10, 2, 256)
+  return -1;
+}
+
+// Emulated launch of a Good-Thomas inner-transform shape (gcd(r2, r3) = 1):
+// the library compiles this form for 16 x 15 x 17 only; these shapes check
+// the kernel's index arithmetic for other radix orders.
+int emu_pass3_gt(EMU_ARGS) {
+  gl_pass_args a{};
+  a.in = in; a.out = out;
+  a.in_ls = in_ls; a.in_is = in_is; a.out_ls = out_ls; a.out_is = out_is;
+  a.lanes = lanes; a.flags = flags; a.tw_m = tw_m; a.tw_r2 = tw_r2; a.tw_lo = tw_lo; a.tw_hi = tw_hi;
+  a.tw_lane_div = tw_lane_div; a.in_limit = in_limit;
+  a.itw_lo = itw_lo; a.itw_hi = itw_hi; a.itw_jmul = itw_jmul;
+  a.dbg_in_words = g_dbg_in; a.dbg_out_words = g_dbg_out; a.dbg_err = &g_dbg_err;
+  a.tw_unscale = g_tw_unscale;
+  const unsigned gx = (lanes + 3) / 4;
+#define SHAPEG(R1, R2, R3, NT)                                                       \
+  if (r1 == R1 && r2 == R2 && r3 == R3) {                                              \
+    if (inv) run_grid<R1, R2, R3, 4, NT, true, true>(a, gx, 1, 1);                     \
+    else run_grid<R1, R2, R3, 4, NT, false, true>(a, gx, 1, 1);                        \
+    return 0;                                                                          \
+  }
+  SHAPEG(8, 5, 17, 256)
+  SHAPEG(8, 3, 17, 256)
+  SHAPEG(16, 16, 3, 256)
+  SHAPEG(16, 15, 2, 256)
+  SHAPEG(16, 17, 2, 256)
   return -1;
 }
 

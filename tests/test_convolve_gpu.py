@@ -26,7 +26,9 @@ def test_reference_kat(gl, oracle, cuda, montgomery):
 @pytest.mark.parametrize("n,count,shared", [(1, 7, False), (1, 5, True), (2, 3, False), (16, 9, True),
                                             (60, 4, False), (4096, 3, True), (3 << 10, 2, False),
                                             (1 << 14, 3, True), (1 << 16, 2, False),
-                                            (255 << 8, 2, True), (1 << 20, 1, True)])
+                                            (255 << 8, 2, True), (1 << 20, 1, True),
+                                            # product fused into a Good-Thomas row pass
+                                            (17 << 16, 1, False), (15 << 14, 2, True)])
 @pytest.mark.parametrize("montgomery", [True, False])
 def test_matches_oracle(gl, oracle, cuda, n, count, shared, montgomery):
     a = rand_field(n * count, seed=n + count)

@@ -28,7 +28,7 @@ def build_emu(tmp_path_factory, extra=()):
     lib.emu_check_flags.restype = ctypes.c_uint32
     lib.emu_set_unscale.argtypes = [ctypes.c_uint64]
     vp, i64, u32, u64 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint64
-    for f in (lib.emu_pass3, lib.emu_generic):
+    for f in (lib.emu_pass3, lib.emu_pass3_gt, lib.emu_generic):
         f.argtypes = [ctypes.c_int] * 4 + [vp, vp, i64, i64, i64, i64, u32, u32,
                                            vp, vp, vp, vp, u32, u32, vp, vp, u64]
     return lib
@@ -63,14 +63,17 @@ def table(w, count, scale=1):
 def call(emu, shape, inv, x, out, in_ls, in_is, out_ls, out_is, lanes, flags, tw_m, tw_r2,
          tw_lo=None, tw_hi=None, lane_div=1, in_limit=NOLIM, itw_lo=None, itw_hi=None, jmul=0,
          unscale=1):
-    """`shape` = (r1, r2, r3) of a compiled kernel, or ("gen", r1, r2, r3) for
-    the run-time-radix kernel.  `unscale` is the inverse of the scale tw_lo
+    """`shape` = (r1, r2, r3) of a compiled kernel, ("gt", r1, r2, r3) for its
+    Good-Thomas inner-transform form, or ("gen", r1, r2, r3) for the
+    run-time-radix kernel.  `unscale` is the inverse of the scale tw_lo
     carries (1: unscaled)."""
     ptr = lambda a: None if a is None else a.ctypes.data
     emu.emu_set_unscale(0 if unscale == 1 else unscale * 2**64 % P)
     fn = emu.emu_pass3
     if shape[0] == "gen":
         fn, shape = emu.emu_generic, shape[1:]
+    elif shape[0] == "gt":
+        fn, shape = emu.emu_pass3_gt, shape[1:]
     rc = fn(*shape, int(inv), ptr(x), ptr(out), in_ls, in_is, out_ls, out_is, lanes, flags,
                        ptr(tw_m), ptr(tw_r2), ptr(tw_lo), ptr(tw_hi), lane_div, in_limit,
                        ptr(itw_lo), ptr(itw_hi), jmul)
@@ -79,11 +82,13 @@ def call(emu, shape, inv, x, out, in_ls, in_is, out_ls, out_is, lanes, flags, tw
 
 @pytest.mark.parametrize("shape", [(8, 8, 1), (16, 16, 1), (8, 8, 8), (16, 8, 8), (16, 16, 6),
                                    (16, 17, 1), (8, 5, 17), (16, 10, 2),
+                                   ("gt", 8, 5, 17), ("gt", 8, 3, 17), ("gt", 16, 16, 3), ("gt", 16, 15, 2),
+                                   ("gt", 16, 17, 2),
                                    ("gen", 3, 1, 1), ("gen", 17, 1, 1), ("gen", 17, 15, 1),
                                    ("gen", 12, 10, 1), ("gen", 5, 6, 17), ("gen", 17, 16, 15)])
 @pytest.mark.parametrize("inv", [False, True])
 def test_whole_transforms_on_columns(emu, oracle, shape, inv):
-    r = shape[1:] if shape[0] == "gen" else shape
+    r = shape[1:] if shape[0] in ("gen", "gt") else shape
     m = r[0] * r[1] * r[2]
     cols = 5
     x = rand_field(m * cols, seed=m + inv)
@@ -168,6 +173,21 @@ def test_four_step_run_time_radices(emu, oracle, inv):
     n1, n2 = 255, 64
     x = rand_field(n1 * n2, seed=17 + inv)
     got = four_step(emu, n1, n2, ("gen", 17, 15, 1), ("gen", 16, 4, 1), x, inv)
+    assert np.array_equal(got, (oracle.intt if inv else oracle.ntt)(x))
+
+
+@pytest.mark.parametrize("inv", [False, True])
+def test_four_step_good_thomas_rows(emu, oracle, inv):
+    """The row pass in the Good-Thomas form (no twiddle between rounds 2 and
+    3; outputs at k1 + R1 * CRT(k2, k3)): 64 x 680 (rows 8 x 5 x 17) and
+    64 x 768 (rows 16 x 16 x 3)."""
+    n1, n2 = 64, 680
+    x = rand_field(n1 * n2, seed=31 + inv)
+    got = four_step(emu, n1, n2, (8, 8, 1), ("gt", 8, 5, 17), x, inv)
+    assert np.array_equal(got, (oracle.intt if inv else oracle.ntt)(x))
+    n1, n2 = 64, 768
+    x = rand_field(n1 * n2, seed=37 + inv)
+    got = four_step(emu, n1, n2, (8, 8, 1), ("gt", 16, 16, 3), x, inv)
     assert np.array_equal(got, (oracle.intt if inv else oracle.ntt)(x))
 
 

@@ -34,7 +34,7 @@ def _defaults(gl):
     (17 << 16, "col 512 (8x8x8, 4 lanes) + row 2176 (16x8x17, 4 lanes)"),
     (1 << 22, "col 2048 (16x16x8, 2 lanes) + row 2048 (16x16x8, 2 lanes)"),
     (1 << 24, "col 4096 (16x16x16, 4 lanes) + row 4096 (16x16x16, 4 lanes)"),
-    (16711680, "col 4096 (16x16x16, 4 lanes) + row 4080 (16x15x17, 4 lanes)"),
+    (16711680, "col 4096 (16x16x16, 4 lanes) + row 4080 (16x15x17, 4 lanes, Good-Thomas)"),
     (15 << 20, "col 4096 (16x16x16, 4 lanes) + row 3840 (16x16x15, 4 lanes)"),
 ])
 def test_two_pass_defaults(gl, n, want):
