@@ -27,7 +27,6 @@ def test_reference_kat(gl, oracle, cuda, montgomery):
                                             (60, 4, False), (4096, 3, True), (3 << 10, 2, False),
                                             (1 << 14, 3, True), (1 << 16, 2, False),
                                             (255 << 8, 2, True), (1 << 20, 1, True),
-                                            # product fused into a Good-Thomas row pass
                                             (17 << 16, 1, False), (15 << 14, 2, True)])
 @pytest.mark.parametrize("montgomery", [True, False])
 def test_matches_oracle(gl, oracle, cuda, n, count, shared, montgomery):
@@ -36,6 +35,18 @@ def test_matches_oracle(gl, oracle, cuda, n, count, shared, montgomery):
     d = to_dev(cuda, a)
     gl.convolve(d, to_dev(cuda, b), size=n, montgomery=montgomery)
     assert np.array_equal(from_dev(d), oracle.convolve(a, b, size=n, montgomery=montgomery))
+
+
+def test_good_thomas_row_pass(gl, oracle, cuda):
+    """16 711 680 = 4096 x 4080: the product is fused into the 4080-point row
+    pass, which runs its inner 15 x 17 transform in the Good-Thomas form."""
+    n = 16711680
+    assert "Good-Thomas" in gl.strategy(n).describe()
+    a = gl.fill_uniform(n, seed=0xC2, offset=0)
+    b = gl.fill_uniform(n, seed=0xC3, offset=0)
+    d = to_dev(cuda, a)
+    gl.convolve(d, to_dev(cuda, b))
+    assert np.array_equal(from_dev(d), oracle.convolve(a, b))
 
 
 def test_three_pass_size(gl, oracle, cuda):
