@@ -417,16 +417,26 @@ def bench_pow(torch):
 
 def bench_small(gl, torch):
     """The reference's CPU-runnable case: one transform of n = 2^16 and a round
-    trip.  Device-resident time per forward call (200 back to back), the
-    synchronous round trip of a host buffer through the drop-in API, and the
-    oracle's single-thread forward time on the same input."""
+    trip.  Device-resident time per forward call, 200 back to back, through
+    the C ABI (gl_plan_execute_ws with a workspace: the device time, the host
+    issues a call in less) and through the Python API (pl.ntt: bound by its
+    host time); the synchronous round trip of a host buffer through the
+    drop-in API; and the oracle's single-thread forward time on the same
+    input."""
     import numpy as np
     import oracle
+    from goldilocks_gb300 import _lib as L
     n = 1 << 16
     x = gl.fill_uniform(n, seed=0x5EED0001)
     d = torch.from_numpy(x.view(np.int64)).cuda()
     pl = gl.strategy(n)
-    fwd_ms = _time_ms(torch, lambda: pl.ntt(d), 200)
+    lib = L.load()
+    wsb = pl.workspace_bytes(1)
+    ws = torch.empty(max(wsb // 8, 1), dtype=torch.int64, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    args = (pl._h, d.data_ptr(), n, L.GL_FORWARD, ws.data_ptr(), wsb, s)
+    fwd_ms = _time_ms(torch, lambda: lib.gl_plan_execute_ws(*args), 200)
+    py_ms = _time_ms(torch, lambda: pl.ntt(d), 200)
     h = torch.empty(n, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
     h[:] = x
     pl.ntt(h)
@@ -443,8 +453,8 @@ def bench_small(gl, torch):
     for _ in range(5):
         oracle.ntt(x)
     cpu_us = (time.perf_counter() - t) / 5 * 1e6
-    return {"n": n, "fwd_us_device": fwd_ms * 1e3, "roundtrip_us_host_memory": rt_us,
-            "cpu_oracle_fwd_us_1_thread": cpu_us}
+    return {"n": n, "fwd_us_device": fwd_ms * 1e3, "fwd_us_python_api": py_ms * 1e3,
+            "roundtrip_us_host_memory": rt_us, "cpu_oracle_fwd_us_1_thread": cpu_us}
 
 
 def cpu_oracle_k12_rate(seconds=2.0):
