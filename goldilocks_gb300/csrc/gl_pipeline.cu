@@ -2,15 +2,17 @@
 // reference, whose transforms run where the data lives).
 //
 // Each job is one round trip: its buffer is copied to the device once, gets
-// every transform of its op list there, and is copied back once.  A large
-// two-pass transform moves in column blocks (2D copies): its column pass
-// starts on the blocks that have arrived and its last row pass hands output
-// blocks to the copy-out stream as they finish.  Four
-// streams per device -- copy-in, two compute streams, copy-out -- with a
-// ring of `depth` device slots, so job i+1 is copied in while job i computes
-// and job i-1 is copied out.  The host-device link carries both directions at once (on
-// GB300 about 340 GB/s together against about 200 GB/s one way), so the
-// overlap nearly halves the copy time of a plain call per transform.
+// every transform of its op list there, and is copied back once.  Four
+// streams per device -- copy-in, two compute streams, copy-out -- with a ring
+// of `depth` device slots, so job i+1 is copied in while job i computes and
+// job i-1 is copied out.  The host-device link carries both directions at
+// once (on GB300 about 340 GB/s together against about 200 GB/s one way), so
+// the overlap nearly halves the copy time of a plain call per transform.
+// When no earlier call is still running, a large two-pass transform moves in
+// column blocks (2D copies): its column pass starts on the blocks that have
+// arrived and its last row pass hands output blocks to the copy-out stream as
+// they finish.  gl_host_pipeline_submit returns without waiting, so calls
+// queued back to back overlap each other as well.
 #include <algorithm>
 #include <map>
 #include <mutex>
@@ -136,9 +138,9 @@ struct events {
 // records *fin on the copy-out stream once all of them are done.  Nothing
 // here waits for the device, so the work of a later call overlaps this one's:
 // its copy-ins follow this call's copy-ins and its passes this call's passes
-// (each call has its own device block, allocated on the copy-in stream and
-// freed on the copy-out stream).  On an error return the streams have been
-// drained and *fin is not set.
+// (each call has a device block of its own: a cached block whose last use has
+// completed, or a new one).  On an error return the streams have been drained
+// and *fin is not set.
 static int pipeline_enqueue(const gl_host_job *jobs, uint64_t njobs, uint32_t depth,
                             cudaEvent_t *fin) {
   *fin = nullptr;
