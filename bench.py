@@ -138,12 +138,17 @@ KERNEL_SOURCES = ("gl_pass3.cuh", "gl_pass.cuh", "gl_field.cuh", "gl_codelets.cu
 
 
 def kernel_source_sha():
-    """sha256 (first 16 hex digits) of the pass-kernel sources, in a fixed order."""
+    """sha256 (first 16 hex digits) of the pass-kernel sources, in a fixed
+    order, with comments and runs of white space removed (an edit of a
+    comment does not change the kernels)."""
     import hashlib
+    import re
     h = hashlib.sha256()
     for name in KERNEL_SOURCES:
         with open(os.path.join(ROOT, "goldilocks_gb300", "csrc", name), "rb") as f:
-            h.update(name.encode() + b"\0" + f.read())
+            code = re.sub(rb"/\*.*?\*/", b" ", f.read(), flags=re.S)
+        code = re.sub(rb"\s+", b" ", re.sub(rb"//[^\n]*", b" ", code)).strip()
+        h.update(name.encode() + b"\0" + code)
     return h.hexdigest()[:16]
 
 

@@ -46,9 +46,10 @@ struct gl_p3_layout {
   static __device__ __forceinline__ int word(int c, int p) {
     return c * LS + (POW2 ? (p ^ ((p >> SH) & MSK)) : p);
   }
-  // Shared memory after the tile (words), staged during round 1 and
+  // Shared memory after the tile (words), staged before round 1 and
   // published by the barrier that ends it:
-  //   T2    the round-2 twiddles tw_r2[R1*i], i < R2*R3 (three rounds only);
+  //   T2    the round-2 twiddles tw_r2[R1*i], i < R2*R3 (three rounds, the
+  //         Cooley-Tukey form only);
   //   STEP  per lane c and last-round output digit t, the pass-twiddle step
   //         omega_n^(col_c * SL * t) (SL: output stride of the last digit),
   //         RL + 1 words per lane so that the lanes fall on distinct banks.
