@@ -303,6 +303,18 @@ static int run_time_passes(const gl_choice &c) {
 gl_choice gl_choice_default(uint64_t n) {
   gl_choice c;
   if (n <= 1) { c.kind = 0; return c; }
+  // 4096 points: two 64-point passes rather than the whole-transform kernel
+  // (three 16-point rounds per CTA).  Measured on GB300 through the C ABI,
+  // calls back to back: one transform 8.2 against 12.3 us, 64 at once 10.3
+  // against 12.3 us, 1 024 at once 51 against 60 us, 4 096 at once 188
+  // against 203 us.
+  if (n == 4096) {
+    c.kind = 2;
+    c.n1 = 64;
+    c.n2 = 64;
+    c.lanes4 = 1;
+    return c;
+  }
   if (gl_find_kernel(n, true, false)) { c.kind = 1; return c; }
   // Four-step with a short first (column) pass and four-lane kernels: 512
   // points when the rest is 128..4096 points (2^16..2^21 and the mixed

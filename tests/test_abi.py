@@ -69,5 +69,6 @@ def test_fill_uniform_is_seeded_and_reduced(gl):
 
 
 def test_workspace_sizes(gl):
-    assert gl.strategy(4096).workspace_bytes(3) == 0
+    assert gl.strategy(2048).workspace_bytes(3) == 0            # one pass
+    assert gl.strategy(4096).workspace_bytes(3) == 8 * 4096 * 3  # two 64-point passes
     assert gl.strategy(1 << 24).workspace_bytes(1) == 8 << 24

@@ -24,6 +24,7 @@ def _defaults(gl):
 
 
 @pytest.mark.parametrize("n,want", [
+    (1 << 12, "col 64 (8x8x1, 4 lanes) + row 64 (8x8x1, 4 lanes)"),
     (1 << 13, "col 64 (8x8x1, 4 lanes) + row 128 (16x8x1, 4 lanes)"),
     (1 << 15, "col 64 (8x8x1, 4 lanes) + row 512 (8x8x8, 4 lanes)"),
     (1 << 16, "col 512 (8x8x8, 4 lanes) + row 128 (16x8x1, 4 lanes)"),

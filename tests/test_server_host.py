@@ -10,7 +10,7 @@ def test_footprint_of_transforms_and_lde(gl):
     assert S.request_bytes(S.GL_OP_NTT, n, cols) == n * cols * 8
     assert S.request_bytes(S.GL_OP_INTT, n, cols) == n * cols * 8
     # a single-pass transform needs none
-    assert S.request_bytes(S.GL_OP_NTT, 4096, cols) == 0
+    assert S.request_bytes(S.GL_OP_NTT, 2048, cols) == 0
     # LDE: the coefficients plus the scratch of the larger (blown-up) transform
     assert S.request_bytes(S.GL_OP_LDE, n, cols, blowup=4) == (n * cols + 4 * n * cols) * 8
 
