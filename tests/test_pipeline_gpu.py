@@ -85,3 +85,30 @@ def test_submitted_calls_overlap_and_match_oracle(gl, oracle, cuda):
         for d in dirs:
             want = (oracle.ntt if d == "fwd" else oracle.intt)(want)
         assert np.array_equal(h, want), (n, dirs)
+
+
+def test_stream_of_calls_reuses_device_blocks(gl, cuda):
+    """Two calls in flight at a time, twenty calls: the pipeline reuses its
+    device blocks once their last use has completed, so free device memory
+    does not shrink after the first calls (a pool that does not reuse blocks
+    freed on another stream grew by one block per call)."""
+    n = 1 << 22
+    xs = [gl.fill_uniform(n, seed=0x57 + s) for s in range(2)]
+    sets = [pinned(cuda, x) for x in xs]
+
+    def run(k):
+        pend = None
+        for i in range(k):
+            t = gl.host_pipeline_submit([(sets[i % 2], n, ("fwd", "inv"))])
+            if pend is not None:
+                pend.wait()
+            pend = t
+        pend.wait()
+    run(6)
+    cuda.cuda.synchronize()
+    free0 = cuda.cuda.mem_get_info()[0]
+    run(20)
+    cuda.cuda.synchronize()
+    assert cuda.cuda.mem_get_info()[0] >= free0 - (16 << 20)
+    for h, x in zip(sets, xs):
+        assert np.array_equal(h, x)  # forward then inverse: the inputs again
