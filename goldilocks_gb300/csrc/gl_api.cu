@@ -956,12 +956,15 @@ extern "C" int gl_debug_check_status(uint32_t *flags) {
 // `dst` may be equal.  Two-pass plans use `scratch` (>= n*C*B words).
 int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64_t C, uint64_t B,
                          uint64_t bs, bool inv, uint64_t *scratch, cudaStream_t stream,
-                         const gl_load_opts *lo, const gl_store_mul *om) {
+                         const gl_load_opts *lo, const gl_store_mul *om, uint64_t out_row) {
   if (B == 0 || C == 0) return GL_OK;
   const uint64_t n = pl->size;
   gl_load_opts none;
   if (!lo) lo = &none;
   if (om && (C != 1 || pl->kind == 0)) return GL_ERR_INVALID;  // contiguous transforms only
+  const uint64_t Co = out_row ? out_row : C;  // words between consecutive output indices
+  if (Co < C || (Co != C && (pl->kind == 0 || pl->kind == 4 || om))) return GL_ERR_INVALID;
+  const uint64_t out_ext = (n - 1) * Co + C;  // words one transform's output spans
   if (pl->kind == 4) {
     if (om || lo->itw_lo || lo->in_limit != 0xffffffffu) return GL_ERR_INVALID;
     return gl_rader_enqueue(pl, src, dst, C, B, bs, inv, scratch, stream);
@@ -1005,7 +1008,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
     }
     if (C == 1) {
       // Lanes are batch items (stride bs).
-      a.in_ls = a.out_ls = (int64_t)bs; a.in_is = a.out_is = 1;
+      a.in_ls = a.out_ls = (int64_t)bs; a.in_is = 1; a.out_is = (int64_t)Co;
       if (coset) { a.itw_jmul = 1; a.tw_lane_div = 0xffffffffu; }
       if (om) { a.flags |= mul_flags; a.mul_ls = mul_item; }  // lane = batch item
       const uint64_t per = (uint64_t)k->lanes * 0x7fffffffull;
@@ -1014,12 +1017,12 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
         a.in = src + off * bs; a.out = dst + off * bs;
         if (om) a.mul = om->factors + off * mul_item;
         a.lanes = (uint32_t)c;
-        GL_DBG_EXTENTS(a, (c - 1) * bs + n, (c - 1) * bs + n);
+        GL_DBG_EXTENTS(a, (c - 1) * bs + n, (c - 1) * bs + out_ext);
         gl_launch(k, 0, a, dim3((unsigned)((c + k->lanes - 1) / k->lanes)), c * n, stream);
       }
     } else {
       // Lanes are the C interleaved columns; batch items on grid.y.
-      a.in_ls = a.out_ls = 1; a.in_is = a.out_is = (int64_t)C;
+      a.in_ls = a.out_ls = 1; a.in_is = (int64_t)C; a.out_is = (int64_t)Co;
       a.in_bs = a.out_bs = (int64_t)bs;
       a.flags |= GL_PF_LOAD_LANE_FAST | GL_PF_STORE_LANE_FAST;
       if (coset) { a.itw_jmul = 1; a.tw_lane_div = 0xffffffffu; }
@@ -1027,7 +1030,7 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       for (uint64_t off = 0; off < B; off += kMaxGridYZ) {
         const uint64_t c = std::min(kMaxGridYZ, B - off);
         a.in = src + off * bs; a.out = dst + off * bs;
-        GL_DBG_EXTENTS(a, (c - 1) * bs + n * C, (c - 1) * bs + n * C);
+        GL_DBG_EXTENTS(a, (c - 1) * bs + n * C, (c - 1) * bs + out_ext);
         gl_launch(k, 0, a, dim3((unsigned)((C + k->lanes - 1) / k->lanes), (unsigned)c),
                c * n * C, stream);
       }
@@ -1083,11 +1086,11 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       c.tw_m = c.tw_r2 = t->blk3[d];
       c.flags = GL_PF_STORE_LANE_FAST;
       c.in = s1; c.out = out;
-      GL_DBG_EXTENTS(c, n * C, n * C);
+      GL_DBG_EXTENTS(c, n * C, out_ext);
       if (C == 1) {
         c.in_ls = (int64_t)n3; c.in_is = 1;                       // lanes: rows k2 of block k1
-        c.out_ls = (int64_t)n1; c.out_is = (int64_t)(n1 * n2);
-        c.in_bs = (int64_t)n23; c.out_bs = 1;                     // grid.y: k1
+        c.out_ls = (int64_t)(n1 * Co); c.out_is = (int64_t)(n1 * n2 * Co);
+        c.in_bs = (int64_t)n23; c.out_bs = (int64_t)Co;           // grid.y: k1
         c.lanes = (uint32_t)n2;
         if (om) {  // output offset k1 + n1 k2 + n1 n2 k3 is the frequency index
           c.flags |= mul_flags;
@@ -1097,9 +1100,9 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
         gl_launch(kcr, 2, c, dim3((unsigned)gl_tiles(n2, kcr), (unsigned)n1), n, stream, true);
       } else {
         c.in_ls = 1; c.in_is = (int64_t)C;                        // lanes: columns
-        c.out_ls = 1; c.out_is = (int64_t)(n1 * n2 * C);
-        c.in_bs = (int64_t)(n3 * C); c.out_bs = (int64_t)(n1 * C);      // grid.y: k2
-        c.in_bs2 = (int64_t)(n23 * C); c.out_bs2 = (int64_t)C;          // grid.z: k1
+        c.out_ls = 1; c.out_is = (int64_t)(n1 * n2 * Co);
+        c.in_bs = (int64_t)(n3 * C); c.out_bs = (int64_t)(n1 * Co);     // grid.y: k2
+        c.in_bs2 = (int64_t)(n23 * C); c.out_bs2 = (int64_t)Co;         // grid.z: k1
         c.flags |= GL_PF_LOAD_LANE_FAST;
         c.lanes = (uint32_t)C;
         gl_launch(kcr, 2, c, dim3((unsigned)gl_tiles(C, kcr), (unsigned)n2,
@@ -1144,10 +1147,10 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
     b.in_limit = 0xffffffffu;  // zero padding applies to the first pass only
     b.tw_m = b.tw_r2 = t->blk[1][d];
     b.flags = GL_PF_STORE_LANE_FAST;
-    GL_DBG_EXTENTS(b, cb * n * C, (cb - 1) * bs + n * C);
+    GL_DBG_EXTENTS(b, cb * n * C, (cb - 1) * bs + out_ext);
     if (C == 1) {
       b.in = scratch + off * n; b.out = dst + off * bs;
-      b.in_ls = (int64_t)n2; b.in_is = 1; b.out_ls = 1; b.out_is = (int64_t)n1;
+      b.in_ls = (int64_t)n2; b.in_is = 1; b.out_ls = (int64_t)Co; b.out_is = (int64_t)(n1 * Co);
       b.in_bs = (int64_t)n; b.out_bs = (int64_t)bs;
       b.lanes = (uint32_t)n1;
       if (om) {  // output offset k1 + n1 k2 is the frequency index
@@ -1158,8 +1161,8 @@ int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64
       gl_launch(kr, 2, b, dim3((unsigned)gl_tiles(n1, kr), (unsigned)cb), cb * n, stream, true);
     } else {
       b.in = scratch + off * n * C; b.out = dst + off * bs;
-      b.in_ls = 1; b.in_is = (int64_t)C; b.out_ls = 1; b.out_is = (int64_t)(n1 * C);
-      b.in_bs = (int64_t)(n2 * C); b.out_bs = (int64_t)C;        // grid.y: k1
+      b.in_ls = 1; b.in_is = (int64_t)C; b.out_ls = 1; b.out_is = (int64_t)(n1 * Co);
+      b.in_bs = (int64_t)(n2 * C); b.out_bs = (int64_t)Co;       // grid.y: k1
       b.in_bs2 = (int64_t)(n * C); b.out_bs2 = (int64_t)bs;      // grid.z: batch
       b.flags |= GL_PF_LOAD_LANE_FAST;
       b.lanes = (uint32_t)C;
@@ -1489,6 +1492,19 @@ static int coset_tables(uint64_t g, uint64_t n, const uint64_t **lo, const uint6
 }
 
 // Device part of the LDE: in (n x cols) -> out (blowup*n x cols), row-major.
+// Coefficient counts from which the LDE runs one length-n transform per coset
+// (below, one zero-padded transform of length blowup * n).
+static const uint64_t kLdeSplitMin = 1ull << 16;
+
+static bool lde_per_coset(const gl_plan *pn, uint64_t n, uint32_t blowup) {
+  return blowup > 1 && n >= kLdeSplitMin && pn->kind >= 1 && pn->kind <= 3;
+}
+
+uint64_t gl_lde_scratch_words(gl_plan *pn, gl_plan *pm, uint64_t n, uint64_t cols, uint32_t blowup) {
+  const uint64_t sn = gl_plan_scratch_words(pn, cols, 1);
+  return lde_per_coset(pn, n, blowup) ? sn : std::max(sn, gl_plan_scratch_words(pm, cols, 1));
+}
+
 static int lde_device(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t cols,
                       uint32_t blowup, uint64_t shift, cudaStream_t stream) {
   const uint64_t m = n * (uint64_t)blowup;
@@ -1506,7 +1522,7 @@ static int lde_device(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t co
   if ((st = coset_tables(shift % GL_P, n, &clo, &chi)) != GL_OK) return st;
   // Coefficients (n x cols) plus scratch for the larger of the two transforms.
   const uint64_t nc = n * cols, mc = m * cols;
-  const uint64_t scratch_words = std::max(gl_plan_scratch_words(pn, cols, 1), gl_plan_scratch_words(pm, cols, 1));
+  const uint64_t scratch_words = gl_lde_scratch_words(pn, pm, n, cols, blowup);
   gl_tmp tmp;
   if ((st = tmp.alloc((nc + scratch_words) * sizeof(uint64_t), stream)) != GL_OK) return st;
   uint64_t *coef = tmp.u64(), *scr = tmp.u64() + nc;
@@ -1519,6 +1535,28 @@ static int lde_device(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t co
   if (pm->kind == 0) {  // m == 1: the value is the constant coefficient
     cudaError_t e = cudaMemcpyAsync(out, coef, nc * 8, cudaMemcpyDeviceToDevice, stream);
     return gl_cuda_status(e);
+  }
+  // Large n: the blowup-times-longer transform of a zero-padded input is
+  // `blowup` transforms of length n, one per coset of the n-th roots:
+  //   X[b j + k] = sum_i c_i (g w^k)^i omega_n^(i j),  w = omega_(b n), k < b,
+  // each reading the n coefficients with the factor (g w^k)^i on load and
+  // writing every b-th output row.  Fewer butterfly stages per output
+  // (log2 n against log2 (b n)) for the same number of HBM passes.
+  if (lde_per_coset(pn, n, blowup)) {
+    const uint64_t w = h_root(m, false);
+    uint64_t h = shift % GL_P;
+    for (uint32_t k = 0; k < blowup; k++) {
+      const uint64_t *hlo = nullptr, *hhi = nullptr;
+      if ((st = coset_tables(h, n, &hlo, &hhi)) != GL_OK) return st;
+      gl_load_opts lk;
+      lk.itw_lo = hlo;
+      lk.itw_hi = hhi;
+      st = gl_enqueue_transform(pn, coef, out + (uint64_t)k * cols, cols, 1, nc, false, scr, stream, &lk,
+                                nullptr, (uint64_t)blowup * cols);
+      if (st != GL_OK) return st;
+      h = h_mul(h, w);
+    }
+    return GL_OK;
   }
   if (!fused) {
     if ((st = gl_coset_pad(coef, out, n, m, cols, clo, chi, stream)) != GL_OK) return st;

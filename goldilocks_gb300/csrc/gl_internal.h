@@ -179,6 +179,8 @@ void gl_launch(const gl_kernel_entry *k, int role, const gl_pass_args &a, dim3 g
 int gl_cuda_status(cudaError_t e);
 void gl_init_mempool_once();
 int gl_sm_count();  // multiprocessors of the current device
+// Scratch words gl_coset_lde takes beside the n x cols coefficients.
+uint64_t gl_lde_scratch_words(gl_plan *pn, gl_plan *pm, uint64_t n, uint64_t cols, uint32_t blowup);
 void gl_pipeline_release_blocks();  // idle device blocks cached by gl_host_pipeline (gl_pipeline.cu)
 
 // Optional load-side transformation (the LDE's zero padding and coset shift).
@@ -227,9 +229,13 @@ int gl_coset_pad(const uint64_t *coef, uint64_t *dst, uint64_t n, uint64_t m, ui
 // Queue the transform of a strided batch on `stream`.  Element j of column c
 // of batch item b is at base[b*bs + j*C + c]; `src` and `dst` may be equal;
 // plans of two or three passes use `scratch` (>= n*C*B words).  (gl_api.cu)
+// out_row: words between consecutive output indices of a transform (0: C,
+// i.e. the input's layout); the LDE writes every blowup-th row with it.  Not
+// for Rader plans.
 int gl_enqueue_transform(gl_plan *pl, const uint64_t *src, uint64_t *dst, uint64_t C, uint64_t B,
                          uint64_t bs, bool inv, uint64_t *scratch, cudaStream_t stream,
-                         const gl_load_opts *lo = nullptr, const gl_store_mul *om = nullptr);
+                         const gl_load_opts *lo = nullptr, const gl_store_mul *om = nullptr,
+                         uint64_t out_row = 0);
 
 // Queue a batch on the persistent kernel without waiting; the kernel's error
 // word (0 = success) is copied to *err_out afterwards.  (gl_batch.cu)

@@ -105,9 +105,8 @@ int footprint(const gl_request &r, uint64_t *bytes) {
     if (r.blowup == 0) return GL_ERR_INVALID;
     gl_plan *pm = nullptr;
     if ((st = gl_plan_create(r.n * (uint64_t)r.blowup, &pm)) != GL_OK) return st;
-    // coefficients (n x cols) + scratch of the larger transform
-    *bytes = (r.n * r.cols + std::max(gl_plan_scratch_words(pn, r.cols, 1),
-                                      gl_plan_scratch_words(pm, r.cols, 1))) * 8;
+    // coefficients (n x cols) + the LDE's scratch
+    *bytes = (r.n * r.cols + gl_lde_scratch_words(pn, pm, r.n, r.cols, r.blowup)) * 8;
   } else {
     *bytes = gl_plan_scratch_words(pn, r.cols, 1) * 8;  // scratch of the transform
   }

@@ -50,6 +50,20 @@ def test_lde_matches_oracle(gl, oracle, cuda, n, cols, blowup):
     assert np.array_equal(from_dev(out), oracle.coset_lde(x, n, cols, blowup, 7))
 
 
+# From 2^16 coefficients the LDE runs one length-n transform per coset of the
+# n-th roots (rows b j + k of the output), reading the coefficients with the
+# factor (g w^k)^i: two-pass and three-pass-free lengths, one and several
+# columns, mixed radix, blowups 2 to 8.
+@pytest.mark.parametrize("n,cols,blowup", [(1 << 16, 3, 4), (1 << 17, 1, 2), (3 << 16, 2, 4),
+                                           (1 << 16, 1, 8), (17 << 12, 5, 2)])
+def test_lde_per_coset_transforms(gl, oracle, cuda, n, cols, blowup):
+    x = rand_field(n * cols, seed=n + cols + blowup)
+    d = to_dev(cuda, x)
+    out = cuda.empty(n * blowup * cols, dtype=cuda.int64, device="cuda")
+    lde_call(gl, cuda, d, out, n, cols, blowup, 7)
+    assert np.array_equal(from_dev(out), oracle.coset_lde(x, n, cols, blowup, 7))
+
+
 def test_lde_host_memory_and_shift(gl, oracle):
     n, cols, blowup, shift = 1024, 3, 4, 2717
     x = rand_field(n * cols, seed=5)

@@ -11,8 +11,12 @@ def test_footprint_of_transforms_and_lde(gl):
     assert S.request_bytes(S.GL_OP_INTT, n, cols) == n * cols * 8
     # a single-pass transform needs none
     assert S.request_bytes(S.GL_OP_NTT, 2048, cols) == 0
-    # LDE: the coefficients plus the scratch of the larger (blown-up) transform
-    assert S.request_bytes(S.GL_OP_LDE, n, cols, blowup=4) == (n * cols + 4 * n * cols) * 8
+    # LDE: the coefficients plus scratch; from 2^16 coefficients one length-n
+    # transform per coset (scratch n x cols), below that one zero-padded
+    # transform of length 4n (scratch 4n x cols)
+    assert S.request_bytes(S.GL_OP_LDE, n, cols, blowup=4) == (n * cols + n * cols) * 8
+    m = 1 << 14
+    assert S.request_bytes(S.GL_OP_LDE, m, cols, blowup=4) == (m * cols + 4 * m * cols) * 8
 
 
 def test_invalid_requests(gl):
